@@ -1,0 +1,353 @@
+"""Benchmark of the SW2D time-stepping core on GB300.
+
+Workload (the synthetic-catchment configuration): a 2048 x 2048 grid, dx = 5 m,
+DEM = tilted plane (slope 0.01 toward the south edge) + seeded 6-octave fractal
+noise (amplitude 2 m, persistence 0.5) + a 3-cell carved channel, Manning n
+from 4 land-use classes by seeded Voronoi patches, uniform rain 50 mm/h for
+t < 3600 s, open south edge, CFL 0.5.  The state is spun up (untimed) to
+t = 1800 s, mid-storm, when every active cell is wet.
+
+One bench step = one replay of the CUDA graph of 48 solver iterations (each
+iteration advances every cell by one time step Dt = 2 dt).  Metric:
+cell-updates/s = active cells x iterations / time.  The L2 cache (129 MB) is
+flushed between bench steps by writing a 256 MB buffer on the solver's stream.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU oracle (the serial C restatement of the
+reference update, OpenMP over rows, FP64) on the host cores, on a bounded
+sample of the same workload.  Under torchrun every rank runs an independent
+replica on its own GPU (the scenarios share nothing), rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "sw2d-gpu_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+CHUNK = 48               # solver iterations per bench step (one graph replay)
+SIZE = 2048
+DX = 5.0
+SEED = 20240
+RAIN_MM_H = 50.0
+RAIN_HOURS = 1.0
+SPINUP_T = 1800.0
+DT_MAX = 1.0             # largest half step [s]
+B_ALG_F32 = 32           # algorithmic bytes per cell-update: read h,um,vn,z,n + write h,um,vn (FP32)
+B_ALG_F64 = 64
+METRIC = "cell-updates/s"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def scenario(seed):
+    from sw2d import scenarios as S
+    return S.catchment(SIZE, dx=DX, seed=seed)
+
+
+def make_solver(sw2d, s, precision, device):
+    g = sw2d.Solver(rows=SIZE, cols=SIZE, dx=DX, dy=DX, precision=precision, dt_mode=sw2d.DT_CFL, dt=DT_MAX,
+                    cfl=0.5, south_open=1, device=device)
+    g.set_static(s["z"], s["n"])
+    g.set_rain(sw2d.RAIN_STEP, [RAIN_MM_H] * int(RAIN_HOURS), 3600.0)
+    return g
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        load = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_cell_update():
+    """DRAM bytes per cell-update of the FP32 step kernel from the committed
+    ncu summary (dram__bytes_read.sum + dram__bytes_write.sum of one launch
+    divided by the cells it updates), or None."""
+    p = os.path.join(ROOT, "profiles", "step_f32_catchment.dram.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_cell_update:"):
+            return float(line.split(":")[1])
+    return None
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import sw2d
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    dev = local
+    torch.cuda.set_device(dev)
+    sw2d.load()
+    s = scenario(SEED + rank)
+    active = int(np.count_nonzero(s["z"] != -9999.0))
+
+    g = make_solver(sw2d, s, sw2d.PREC_F32, dev)
+    g.set_state(s["h0"])
+    t0 = time.time()
+    g.advance(10 ** 9, t_end=SPINUP_T)
+    log(f"[rank {rank}] spin-up to t={SPINUP_T}s: {g.budget()['steps']} iterations, {time.time() - t0:.1f}s wall")
+    spun = g.state()
+
+    stream = torch.cuda.ExternalStream(g.stream())
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")
+
+    def timed_chunks(solver, k, w, per_chunk=CHUNK):
+        st = torch.cuda.ExternalStream(solver.stream())
+        for _ in range(w):
+            solver.advance(per_chunk)
+        times = []
+        for _ in range(k):
+            with torch.cuda.stream(st):
+                flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            n = solver.advance(per_chunk)
+            e1.record(st)
+            e1.synchronize()
+            assert n == per_chunk, f"advance stopped after {n} iterations"
+            times.append(e0.elapsed_time(e1) / 1e3)
+        return times
+
+    # ---- device-timed FP32 (the product path) -------------------------------
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = g.launch_count()
+    sampler = ClockSampler(dev)
+    sampler.start()
+    wall0 = time.perf_counter()
+    times = timed_chunks(g, args.steps, args.warmup)
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop()
+    torch.cuda.synchronize()
+    launches = g.launch_count() - launches0 - args.warmup * CHUNK
+    tot = sum(times)
+    if ws > 1:
+        t = torch.tensor([tot], dtype=torch.float64, device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tot = float(t.item())
+    cu = active * CHUNK * args.steps
+    value = cu * ws / tot
+    per_launch = tot / (CHUNK * args.steps)
+    peak, peak_kind = peaks()
+    achieved = B_ALG_F32 * active / per_launch / 1e9
+    tpc = traffic_per_cell_update()
+    bud = g.budget()
+    vol_err = abs(bud["volume"] - (bud["volume0"] + bud["rain_in"] + bud["source_in"] - bud["evap_out"] -
+                                   bud["outflow"] + bud["clamp_gain"])) / max(bud["volume"], 1e-30)
+    g.close()
+
+    # ---- FP64 plain path on the same spun-up state (secondary) -------------
+    g64 = make_solver(sw2d, s, sw2d.PREC_F64, dev)
+    g64.set_state(spun["h"], spun["um"], spun["vn"], t0=SPINUP_T)
+    t64 = timed_chunks(g64, max(2, args.steps // 40), 1)
+    v64 = active * CHUNK * len(t64) / sum(t64)
+    g64.close()
+
+    # ---- end to end through the C ABI with host buffers ----------------------
+    k_e2e = max(3, args.steps // 4)
+    h_pinned = torch.from_numpy(s["h0"]).pin_memory()
+    z_pinned = torch.from_numpy(s["z"]).pin_memory()
+    n_pinned = torch.from_numpy(s["n"]).pin_memory()
+    spun_pin = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in spun.items()}
+    torch.cuda.synchronize()
+    te0 = time.perf_counter()
+    ge = sw2d.Solver(rows=SIZE, cols=SIZE, dx=DX, dy=DX, precision=sw2d.PREC_F32, dt_mode=sw2d.DT_CFL, dt=DT_MAX,
+                     cfl=0.5, south_open=1, device=dev)
+    ge.set_static(z_pinned.numpy(), n_pinned.numpy())
+    ge.set_rain(sw2d.RAIN_STEP, [RAIN_MM_H], 3600.0)
+    ge.set_state(spun_pin["h"].numpy(), spun_pin["um"].numpy(), spun_pin["vn"].numpy(), t0=SPINUP_T)
+    for _ in range(k_e2e):
+        ge.advance(CHUNK)
+        ge.budget()  # device->host read of the step's result (volume + budgets)
+    out_h = ge.depth()
+    te = time.perf_counter() - te0
+    ge.close()
+    del h_pinned
+    e2e_value = active * CHUNK * k_e2e / te
+    h2d = (SIZE * SIZE * 8) * 2 + (SIZE * SIZE * 8) + ((SIZE + 1) * SIZE * 8) * 2  # z, n, h, um, vn
+    d2h = SIZE * SIZE * 8 + k_e2e * (1024 * 8 + 200)
+    assert np.isfinite(out_h).all()
+
+    # ---- CPU baseline: the oracle on a bounded sample ------------------------
+    cpu = cpu_sample(s, spun, budget_s=args.cpu_seconds) if rank == 0 else None
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "synthetic catchment 2048x2048, dx 5 m, rain 50 mm/h, open south edge, CFL 0.5, "
+                                   "state spun up to t=1800 s; FP32 state, FP64 budgets",
+                       "grid": [SIZE, SIZE], "active_cells": active, "iterations_per_step": CHUNK,
+                       "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{ws}",
+                       "seed": SEED},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": (tpc * active if tpc is not None else None),
+                         "bytes_alg_per_cell_update": B_ALG_F32, "kernel": "step_kernel<float,16,32,256>",
+                         "launch_s": per_launch},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / k_e2e,
+                    "d2h_bytes_per_step": d2h / k_e2e, "steps": k_e2e},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+            "wall_s_timed": wall,
+            "fp64_plain": {"value": v64, "unit": "cell-updates/s", "speedup_f32_over_f64": value / ws / v64},
+            "volume_rel_error": vol_err,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_sample(s, spun, budget_s=12.0):
+    """The CPU oracle on the same workload: the spun-up 2048x2048 state,
+    iterated for about `budget_s` seconds with all host threads."""
+    import oracle as O
+    o = O.Oracle(SIZE, SIZE, DX, DX, s["z"], n=s["n"], dt_mode=1, dt=DT_MAX, cfl=0.5, south_open=1)
+    o.set_state(spun["h"], spun["um"], spun["vn"], t=SPINUP_T)
+    o.set_forcing(O.OracleForcing(rain_kind=O.RAIN_STEP, rain=[RAIN_MM_H], rain_dt=3600.0))
+    active = int((s["z"] != -9999.0).sum())
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s:
+        n += o.advance(1)
+    el = time.perf_counter() - t0
+    return {"value": active * n / el, "unit": "cell-updates/s", "cores": O.max_threads(), "kind": "port",
+            "sample": f"{n} iterations of the spun-up 2048x2048 catchment, FP64, {el:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle as O
+    O.build()
+    s = scenario(SEED)
+    o = O.Oracle(SIZE, SIZE, DX, DX, s["z"], n=s["n"], dt_mode=1, dt=DT_MAX, cfl=0.5, south_open=1)
+    o.set_forcing(O.OracleForcing(rain_kind=O.RAIN_STEP, rain=[RAIN_MM_H], rain_dt=3600.0))
+    # the spin-up is not part of the reference arm's timing: start from a
+    # uniform 5 mm film, mid-storm, so that every cell does the full update
+    import numpy as np
+    o.set_state(np.where(s["z"] != -9999.0, 0.005, 0.0), t=SPINUP_T)
+    active = int((s["z"] != -9999.0).sum())
+    per_step = 2  # iterations of the full grid per reference bench step (bounded sample)
+    for _ in range(args.warmup):
+        o.advance(1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.advance(per_step)
+    el = time.perf_counter() - t0
+    value = active * per_step * args.steps / el
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": "synthetic catchment 2048x2048 (the same grid), FP64 reference scheme on host cores",
+                   "grid": [SIZE, SIZE], "active_cells": active, "iterations_per_step": per_step},
+        "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": O.max_threads(), "kind": "port",
+                         "sample": f"{per_step} iterations of the 2048x2048 catchment per step"},
+        "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,196 @@
+/*
+ * sw2d.h -- C ABI of the GB300-native SW2D time-stepping core.
+ *
+ * This is the drop-in boundary for the solver loop of the reference
+ * SW2D-GPU (SW2D-GPU_linux/src/SW2D-GPU.cu, "cu:<line>" below).  The
+ * reference has no library interface: main() allocates 20 raw device arrays
+ * (cu:1163-1190), uploads them (cu:1194-1213), launches nine kernels per
+ * iteration (cu:1256-1336) and copies fields back for output
+ * (cu:1376, 1426, 1442, 1458).  Each entry point below replaces one of those
+ * steps; the comment on each names the reference code it stands in for.
+ *
+ * Conventions
+ *   - Every call returns an int status (sw2d_status); nothing throws across
+ *     the ABI.  sw2d_last_error() gives a message for the last failure.
+ *   - Host arrays are row-major, north row first, float64:
+ *       cells    rows x cols
+ *       x-faces  (rows+1) x cols : um[i][j] is the face between cells
+ *                (i-1,j) and (i,j); the reference's "X-DIRECTION" (cu:113)
+ *       y-faces  rows x (cols+1) : vn[i][j] is the face between cells
+ *                (i,j-1) and (i,j); the reference's "Y-DIRECTION" (cu:229)
+ *     The device layout (pitch, precision) is private to the library.
+ *   - The handle owns its device memory and one CUDA stream; the caller owns
+ *     every host buffer.  A handle is not thread-safe.
+ *   - A cell with elevation == nodata is inactive; all its faces are walls
+ *     (cu:39-44, cu:117-118).
+ */
+#ifndef SW2D_H
+#define SW2D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SW2D_ABI_VERSION 1
+
+typedef enum {
+    SW2D_OK = 0,
+    SW2D_ERR_INVALID_ARG = 1, /* bad size, null pointer, out-of-range value */
+    SW2D_ERR_OOM = 2,         /* device allocation failed */
+    SW2D_ERR_CUDA = 3,        /* any other CUDA runtime error */
+    SW2D_ERR_NONFINITE = 4,   /* a NaN/Inf depth or discharge was produced */
+    SW2D_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+    SW2D_ERR_STATE = 6        /* call order: e.g. advance before set_static */
+} sw2d_status;
+
+enum { SW2D_PREC_F64 = 0, SW2D_PREC_F32 = 1 };
+/* FIXED: the reference's rule, a constant half step dt (cu:790, cu:808),
+ *        loop while t + dt <= t_end (cu:1256).
+ * CFL:   extension; dt2 = min(2*dt, cfl*min(dx,dy)/cmax), clipped to t_end,
+ *        where cmax = max over wet interior faces of |q/h_face| + sqrt(g*h_face)
+ *        of the current state. */
+enum { SW2D_DT_FIXED = 0, SW2D_DT_CFL = 1 };
+
+enum {
+    SW2D_FIELD_DEPTH = 0,     /* h, rows x cols            (reference d_h)   */
+    SW2D_FIELD_UM = 1,        /* x-face discharge, (rows+1) x cols (d_um)   */
+    SW2D_FIELD_VN = 2,        /* y-face discharge, rows x (cols+1) (d_vn)   */
+    SW2D_FIELD_UU = 3,        /* cell velocity along rows, rows x cols (d_uu, cu:473) */
+    SW2D_FIELD_VV = 4,        /* cell velocity along cols, rows x cols (d_vv, cu:474) */
+    SW2D_FIELD_ELEVATION = 5  /* z as stored on the device, rows x cols      */
+};
+
+enum {
+    SW2D_RAIN_NONE = 0,
+    SW2D_RAIN_COMPAT = 1, /* series in mm per interval, the reference's
+                             interpolation formula (cu:547-554) */
+    SW2D_RAIN_STEP = 2,   /* series in mm/h, constant over each interval, 0 after */
+    SW2D_RAIN_LINEAR = 3, /* series in mm/h at knots k*dt, linear, 0 after */
+    SW2D_RAIN_STORM = 4   /* moving Gaussian storm cell (sw2d_set_storm) */
+};
+
+typedef struct {
+    int32_t rows, cols;
+    double dx, dy;          /* cell size [m] (the reference has dx = dy = cellsize, cu:1236) */
+    double nodata;          /* NODATA_value of the DEM (cu:827) */
+    double g;               /* 9.80 in the reference (cu:809) */
+    double th;              /* wet/dry threshold, 1.0e-4 m (cu:1130) */
+    double manning;         /* scalar Manning n (cu:799) when no raster is given */
+    double INT, INF, LWL;   /* runoff fractions of rain (cu:627-634) */
+    double EV_WL_min;       /* depth above which LWL and evaporation apply */
+    int32_t precision;      /* SW2D_PREC_F64 (exact scheme) or SW2D_PREC_F32 */
+    int32_t dt_mode;        /* SW2D_DT_FIXED or SW2D_DT_CFL */
+    double dt;              /* FIXED: the half step; CFL: the largest half step */
+    double cfl;             /* Courant number for SW2D_DT_CFL (0.5) */
+    int32_t south_open;     /* 1: free outfall through the south edge (extension) */
+    int32_t device;         /* CUDA device ordinal */
+    int32_t tile_h, tile_w; /* core tile of the step kernel, 0 = default */
+    int32_t reserved[4];
+} sw2d_config;
+
+typedef struct {
+    double t;          /* simulated time [s] */
+    double dt;         /* half step of the last iteration [s] */
+    double cmax;       /* wave-speed bound of the current state [m/s] */
+    double volume;     /* water on active cells now [m^3], FP64 Kahan sum */
+    double volume0;    /* at sw2d_set_state */
+    double rain_in;    /* cumulative inflows/outflows [m^3], FP64 Kahan */
+    double source_in;
+    double evap_out;
+    double outflow;    /* through the open south edge */
+    double clamp_gain; /* water created by the depth clamp fmax(h,0) (cu:657) */
+    int64_t steps;     /* iterations done since sw2d_set_state */
+    int32_t nonfinite; /* 1 if a non-finite value was produced */
+    int32_t reserved;
+} sw2d_budget;
+
+typedef struct sw2d_handle sw2d_handle;
+
+/* Fills cfg with the reference's constants (g = 9.80, th = 1e-4, FP64,
+ * fixed dt).  Replaces the constants of cu:808-809 and cu:1130. */
+int sw2d_config_init(sw2d_config *cfg);
+
+/* Device bytes a handle with this config allocates (admission control). */
+int sw2d_device_bytes(const sw2d_config *cfg, int64_t *bytes);
+
+/* Creates a handle and allocates all device memory.
+ * Replaces the cudaMalloc block cu:1163-1190 and the launch setup cu:1222-1235. */
+int sw2d_create(const sw2d_config *cfg, sw2d_handle **out);
+
+/* Frees everything.  Replaces cu:1490-1521. */
+int sw2d_destroy(sw2d_handle *h);
+
+/* Uploads the DEM (rows x cols) and an optional per-cell Manning raster
+ * (NULL = cfg.manning everywhere).  Derives the active mask.
+ * Replaces the d_baseo upload (cu:1213) and init_inf (cu:29-49, cu:1238). */
+int sw2d_set_static(sw2d_handle *h, const double *z, const double *manning);
+
+/* Uploads the state at time t0: depth (rows x cols) and optional discharges
+ * um ((rows+1) x cols) and vn (rows x (cols+1)); NULL = zero.  Inactive cells
+ * get depth 0.  Resets budgets and the iteration count.
+ * Replaces the state uploads cu:1194-1210 and initiald (cu:52-92, cu:1240). */
+int sw2d_set_state(sw2d_handle *h, const double *depth, const double *um, const double *vn,
+                   double t0);
+
+/* Uniform rain series (SW2D_RAIN_COMPAT/STEP/LINEAR) or SW2D_RAIN_NONE.
+ * Replaces the rain part of stream_flow (cu:547-554) and the d_rr uploads
+ * (cu:1280, cu:1305). */
+int sw2d_set_rain(sw2d_handle *h, int32_t kind, const double *series, int32_t n, double dt_series);
+
+/* Moving Gaussian storm: rate = peak * exp(-r^2 / (2 sigma^2)) [mm/h] with
+ * centre (x0 + vx t, y0 + vy t); x grows with the column, y with the row
+ * (southwards), both from the north-west corner; zero for t >= t_stop.
+ * Extension (the reference's rain is one scalar, cu:547). */
+int sw2d_set_storm(sw2d_handle *h, double peak_mm_h, double x0, double y0, double vx,
+                   double vy, double sigma, double t_stop);
+
+/* Evaporation series in mm per interval, reference formula
+ * (evaporation_load cu:589-601, d_Ev uploads cu:1284, cu:1309); applied
+ * where the depth is above EV_WL_min (cu:627-634).  n = 0 disables it. */
+int sw2d_set_evaporation(sw2d_handle *h, const double *series_mm, int32_t n, double dt_series);
+
+/* Point sources/sinks: cells[k] is the linear cell index i*cols+j of source
+ * k; q is n_rec x n_src discharges [m^3/s] at interval dtoq, interpolated
+ * with the reference's formula (stream_flow cu:532-546).  When two sources
+ * share a cell the later one wins, as in the reference.  Replaces the d_ql
+ * uploads (cu:1279, cu:1304).  n_src = 0 removes all sources. */
+int sw2d_set_point_sources(sw2d_handle *h, const int32_t *cells, int32_t n_src, const double *q,
+                           int32_t n_rec, double dtoq);
+
+/* Runs iterations of the solver loop until max_steps iterations are done or
+ * the end-time condition fails (FIXED: t + dt <= t_end as in cu:1256; CFL:
+ * t < t_end, last step clipped to land on t_end).  *steps_done (nullable)
+ * receives the count.  Replaces the while loop cu:1256-1336. */
+int sw2d_advance(sw2d_handle *h, int64_t max_steps, double t_end, int64_t *steps_done);
+
+/* Copies a field of the current state to host memory (size per field enum).
+ * Replaces the D2H copies cu:1376, cu:1426, cu:1442, cu:1458; the velocity
+ * fields are computed on demand (uu_vv, cu:459-484). */
+int sw2d_get_field(sw2d_handle *h, int32_t field, double *out);
+
+/* Time, step count and FP64 mass budget of the current state. */
+int sw2d_get_budget(sw2d_handle *h, sw2d_budget *out);
+
+/* Depth at n cells (linear indices).  Replaces the WaterLevel.txt probe
+ * loop cu:1386-1410. */
+int sw2d_probe(sw2d_handle *h, const int32_t *cells, int32_t n, double *out);
+
+/* Waits for all work of the handle.  The stream (a cudaStream_t) is
+ * exposed so that callers can order their own work or time it. */
+int sw2d_synchronize(sw2d_handle *h);
+int sw2d_get_stream(sw2d_handle *h, void **stream);
+
+/* Number of step-kernel launches issued since sw2d_set_state (including
+ * launches that found the run already finished and did no work). */
+int sw2d_launch_count(sw2d_handle *h, int64_t *launches);
+
+const char *sw2d_last_error(const sw2d_handle *h);
+const char *sw2d_status_string(int32_t status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SW2D_H */

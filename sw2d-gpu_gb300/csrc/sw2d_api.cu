@@ -1,0 +1,679 @@
+// sw2d_api.cu -- host implementation of the C ABI declared in include/sw2d.h.
+//
+// A handle owns: the pitched device state in two ping-pong buffers (h, um,
+// vn), the static fields, a float64 staging buffer for uploads/downloads,
+// three rotating Clock slots, the Control block, the forcing tables, one
+// non-blocking stream and a CUDA graph of kChunk step launches that is
+// replayed by sw2d_advance.  Time and time step live on the device, so an
+// advance needs one host synchronisation per chunk, not per iteration (the
+// reference synchronises nine times per iteration, cu:1268-1332).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sw2d.h"
+#include "sw2d_launch.h"
+
+using namespace sw2d;
+
+namespace {
+
+constexpr int kChunk = 48;  // launches per graph replay, a multiple of 3 (clock slots)
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct sw2d_handle {
+    sw2d_config cfg{};
+    int real_size = 8;
+    int pitch = 0;
+    size_t plane = 0;  // elements per pitched array: (rows+1) * pitch
+    int tile_h = 16, tile_w = 32, nblocks = 0;
+    cudaStream_t stream = nullptr;
+    void *h[2] = {nullptr, nullptr}, *um[2] = {nullptr, nullptr}, *vn[2] = {nullptr, nullptr};
+    void *z = nullptr, *nman = nullptr;
+    uint8_t *mask = nullptr;
+    double *stage = nullptr, *stage2 = nullptr;
+    size_t stage_elems = 0;
+    double *partial = nullptr;
+    Clock *d_clk = nullptr;
+    Control *d_ctl = nullptr;
+    Clock *h_clk = nullptr;    // pinned
+    Control *h_ctl = nullptr;  // pinned
+    double *h_partial = nullptr;  // pinned
+    DevBuf rain, ev, src_cell, src_q, probe_cells, probe_out;
+    ForcingDesc F{};
+    GridDesc G{};
+    bool have_static = false, have_state = false, has_nraster = false;
+    long long launches = 0;
+    Clock clock{};  // last clock read back
+    double volume0 = 0.0;
+    cudaGraphExec_t graph = nullptr;
+    bool graph_valid = false;
+    std::string err;
+};
+
+namespace {
+
+int fail(sw2d_handle *h, int code, const std::string &msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+int cuda_fail(sw2d_handle *h, cudaError_t e, const char *what) {
+    const int code = (e == cudaErrorMemoryAllocation) ? SW2D_ERR_OOM : SW2D_ERR_CUDA;
+    return fail(h, code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(h, expr)                                             \
+    do {                                                        \
+        cudaError_t e_ = (expr);                                \
+        if (e_ != cudaSuccess) return cuda_fail((h), e_, #expr); \
+    } while (0)
+
+bool is_f64(const sw2d_handle *h) { return h->cfg.precision == SW2D_PREC_F64; }
+
+template <class Real>
+Real thr_ge(double x) {
+    if (sizeof(Real) == 8) return (Real)x;
+    float f = (float)x;
+    if ((double)f < x) f = std::nextafter(f, INFINITY);
+    return (Real)f;
+}
+
+template <class Real>
+Real thr_gt(double x) {
+    if (sizeof(Real) == 8) return (Real)std::nextafter(x, INFINITY);
+    float f = (float)x;
+    if ((double)f <= x) f = std::nextafter(f, INFINITY);
+    return (Real)f;
+}
+
+template <class Real>
+Thr<Real> make_thr(const sw2d_config &c) {
+    Thr<Real> t;
+    t.gt_th = thr_gt<Real>(c.th);
+    t.ge_th = thr_ge<Real>(c.th);
+    t.gt_evmin = thr_gt<Real>(c.EV_WL_min);
+    return t;
+}
+
+template <class Real>
+StateBufs<Real> make_bufs(const sw2d_handle *h) {
+    StateBufs<Real> s;
+    for (int b = 0; b < 2; b++) {
+        s.h[b] = (Real *)h->h[b];
+        s.um[b] = (Real *)h->um[b];
+        s.vn[b] = (Real *)h->vn[b];
+    }
+    s.z = (const Real *)h->z;
+    s.nman = h->has_nraster ? (const Real *)h->nman : nullptr;
+    s.mask = h->mask;
+    return s;
+}
+
+cudaError_t launch_one(sw2d_handle *h, int slot) {
+    if (is_f64(h))
+        return launch_step(h->tile_h, h->tile_w, h->nblocks, h->G, h->F, make_bufs<double>(h),
+                           make_thr<double>(h->cfg), h->d_clk, h->d_ctl, slot, h->stream);
+    return launch_step(h->tile_h, h->tile_w, h->nblocks, h->G, h->F, make_bufs<float>(h),
+                       make_thr<float>(h->cfg), h->d_clk, h->d_ctl, slot, h->stream);
+}
+
+int validate(const sw2d_config *c, std::string *why) {
+    if (!c) return *why = "config is null", 0;
+    if (c->rows < 1 || c->cols < 1) return *why = "rows and cols must be >= 1", 0;
+    if ((long long)(c->rows + 1) * (c->cols + 33) > (1ll << 31)) return *why = "grid too large for 32-bit indexing", 0;
+    if (!(c->dx > 0) || !(c->dy > 0)) return *why = "dx and dy must be > 0", 0;
+    if (!(c->dt > 0)) return *why = "dt must be > 0", 0;
+    if (c->precision != SW2D_PREC_F64 && c->precision != SW2D_PREC_F32) return *why = "unknown precision", 0;
+    if (c->dt_mode != SW2D_DT_FIXED && c->dt_mode != SW2D_DT_CFL) return *why = "unknown dt_mode", 0;
+    if (c->dt_mode == SW2D_DT_CFL && !(c->cfl > 0)) return *why = "cfl must be > 0", 0;
+    if (!(c->g > 0) || !(c->th >= 0)) return *why = "g must be > 0 and th >= 0", 0;
+    return 1;
+}
+
+void grid_shape(const sw2d_config *c, int *pitch, size_t *plane, int *th, int *tw) {
+    *pitch = ((c->cols + 1 + 31) / 32) * 32;
+    *plane = (size_t)(c->rows + 1) * (size_t)(*pitch);
+    int a = c->tile_h, b = c->tile_w;
+    if (a <= 0 || b <= 0 || !tile_supported(c->precision, a, b)) default_tile(c->precision, &a, &b);
+    *th = a;
+    *tw = b;
+}
+
+int read_clock(sw2d_handle *h) {
+    const int slot = (int)(h->launches % 3);
+    CK(h, cudaMemcpyAsync(h->h_clk, h->d_clk + slot, sizeof(Clock), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->clock = *h->h_clk;
+    return SW2D_OK;
+}
+
+int capture_graph(sw2d_handle *h) {
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int m = 0; m < kChunk && e == cudaSuccess; m++) e = launch_one(h, m % 3);
+    cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+    if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(h, e, "step launch during capture");
+    }
+    if (e2 != cudaSuccess) return cuda_fail(h, e2, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+    h->graph_valid = true;
+    return SW2D_OK;
+}
+
+template <class T>
+int upload_table(sw2d_handle *h, DevBuf &b, const T *src, size_t n) {
+    const size_t bytes = n * sizeof(T);
+    if (bytes > b.bytes) {
+        if (b.p) cudaFree(b.p);
+        b.p = nullptr;
+        b.bytes = 0;
+        CK(h, cudaMalloc(&b.p, bytes));
+        b.bytes = bytes;
+    }
+    if (bytes) CK(h, cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return SW2D_OK;
+}
+
+}  // namespace
+
+namespace sw2d {
+
+bool tile_supported(int precision, int th, int tw) {
+    if (precision == SW2D_PREC_F64) return (th == 16 && tw == 32) || (th == 8 && tw == 32);
+    return (th == 16 && tw == 32) || (th == 32 && tw == 32) || (th == 16 && tw == 64);
+}
+
+void default_tile(int precision, int *th, int *tw) {
+    *th = 16;
+    *tw = 32;
+    (void)precision;
+}
+
+}  // namespace sw2d
+
+extern "C" {
+
+int sw2d_config_init(sw2d_config *c) {
+    if (!c) return SW2D_ERR_INVALID_ARG;
+    std::memset(c, 0, sizeof(*c));
+    c->rows = c->cols = 0;
+    c->dx = c->dy = 1.0;
+    c->nodata = -9999.0;
+    c->g = 9.80;      // cu:809
+    c->th = 1.0e-4;   // cu:1130
+    c->manning = 0.0;
+    c->precision = SW2D_PREC_F64;
+    c->dt_mode = SW2D_DT_FIXED;
+    c->dt = 0.04;
+    c->cfl = 0.5;
+    return SW2D_OK;
+}
+
+int sw2d_device_bytes(const sw2d_config *c, int64_t *bytes) {
+    std::string why;
+    if (!bytes || !validate(c, &why)) return SW2D_ERR_INVALID_ARG;
+    int pitch, th, tw;
+    size_t plane;
+    grid_shape(c, &pitch, &plane, &th, &tw);
+    const size_t rs = c->precision == SW2D_PREC_F64 ? 8 : 4;
+    size_t total = plane * rs * 8;  // 2x(h, um, vn) + z + n
+    total += plane;                 // mask
+    total += 2 * (size_t)(c->rows + 1) * (c->cols + 1) * sizeof(double);  // staging
+    total += kVolumeBlocks * sizeof(double) + 3 * sizeof(Clock) + sizeof(Control);
+    *bytes = (int64_t)total;
+    return SW2D_OK;
+}
+
+int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
+    if (!out) return SW2D_ERR_INVALID_ARG;
+    *out = nullptr;
+    std::string why;
+    if (!validate(cfg, &why)) return SW2D_ERR_INVALID_ARG;
+    sw2d_handle *h = new sw2d_handle();
+    h->cfg = *cfg;
+    h->real_size = cfg->precision == SW2D_PREC_F64 ? 8 : 4;
+    grid_shape(cfg, &h->pitch, &h->plane, &h->tile_h, &h->tile_w);
+    auto bail = [&](int code) {
+        sw2d_destroy(h);
+        return code;
+    };
+    cudaError_t e = cudaSetDevice(cfg->device);
+    if (e != cudaSuccess) return bail(SW2D_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(SW2D_ERR_CUDA);
+    const size_t fb = h->plane * h->real_size;
+    for (int b = 0; b < 2; b++) {
+        void **arrs[3] = {&h->h[b], &h->um[b], &h->vn[b]};
+        for (void **a : arrs) {
+            if (cudaMalloc(a, fb) != cudaSuccess) return bail(SW2D_ERR_OOM);
+            if (cudaMemset(*a, 0, fb) != cudaSuccess) return bail(SW2D_ERR_CUDA);
+        }
+    }
+    if (cudaMalloc(&h->z, fb) != cudaSuccess || cudaMemset(h->z, 0, fb) != cudaSuccess) return bail(SW2D_ERR_OOM);
+    if (cudaMalloc(&h->nman, fb) != cudaSuccess || cudaMemset(h->nman, 0, fb) != cudaSuccess) return bail(SW2D_ERR_OOM);
+    if (cudaMalloc((void **)&h->mask, h->plane) != cudaSuccess || cudaMemset(h->mask, 0, h->plane) != cudaSuccess)
+        return bail(SW2D_ERR_OOM);
+    h->stage_elems = (size_t)(cfg->rows + 1) * (cfg->cols + 1);
+    if (cudaMalloc((void **)&h->stage, h->stage_elems * sizeof(double)) != cudaSuccess) return bail(SW2D_ERR_OOM);
+    if (cudaMalloc((void **)&h->stage2, h->stage_elems * sizeof(double)) != cudaSuccess) return bail(SW2D_ERR_OOM);
+    if (cudaMalloc((void **)&h->partial, kVolumeBlocks * sizeof(double)) != cudaSuccess) return bail(SW2D_ERR_OOM);
+    if (cudaMalloc((void **)&h->d_clk, 3 * sizeof(Clock)) != cudaSuccess) return bail(SW2D_ERR_OOM);
+    if (cudaMalloc((void **)&h->d_ctl, sizeof(Control)) != cudaSuccess) return bail(SW2D_ERR_OOM);
+    if (cudaMallocHost((void **)&h->h_clk, sizeof(Clock)) != cudaSuccess) return bail(SW2D_ERR_OOM);
+    if (cudaMallocHost((void **)&h->h_ctl, sizeof(Control)) != cudaSuccess) return bail(SW2D_ERR_OOM);
+    if (cudaMallocHost((void **)&h->h_partial, kVolumeBlocks * sizeof(double)) != cudaSuccess) return bail(SW2D_ERR_OOM);
+    if (cudaMemset(h->d_clk, 0, 3 * sizeof(Clock)) != cudaSuccess) return bail(SW2D_ERR_CUDA);
+    e = is_f64(h) ? prepare_step(h->tile_h, h->tile_w, 0.0) : prepare_step(h->tile_h, h->tile_w, 0.0f);
+    if (e != cudaSuccess) return bail(SW2D_ERR_CUDA);
+
+    GridDesc &G = h->G;
+    G.rows = cfg->rows;
+    G.cols = cfg->cols;
+    G.pitch = h->pitch;
+    G.tiles_w = (cfg->cols + h->tile_w - 1) / h->tile_w;
+    const int tiles_h = (cfg->rows + h->tile_h - 1) / h->tile_h;
+    h->nblocks = tiles_h * G.tiles_w;
+    G.dt_mode = cfg->dt_mode;
+    G.south_open = cfg->south_open ? 1 : 0;
+    G.n_src = 0;
+    G.dx = cfg->dx;
+    G.dy = cfg->dy;
+    G.g = cfg->g;
+    G.th = cfg->th;
+    G.cfl = cfg->cfl;
+    G.dmin = cfg->dx < cfg->dy ? cfg->dx : cfg->dy;
+    G.dt_half = cfg->dt;
+    G.pct_hi = 1.00 - cfg->LWL;               // cu:628
+    G.pct_lo = 1.00 - (cfg->INT + cfg->INF);  // cu:632
+    G.manning = cfg->manning;
+    h->F.rain_kind = RAIN_NONE;
+    h->F.rain_dt = 1.0;
+    h->F.ev_dt = 1.0;
+    h->F.dtoq = 1.0;
+    *out = h;
+    return SW2D_OK;
+}
+
+int sw2d_destroy(sw2d_handle *h) {
+    if (!h) return SW2D_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    for (int b = 0; b < 2; b++) {
+        cudaFree(h->h[b]);
+        cudaFree(h->um[b]);
+        cudaFree(h->vn[b]);
+    }
+    cudaFree(h->z);
+    cudaFree(h->nman);
+    cudaFree(h->mask);
+    cudaFree(h->stage);
+    cudaFree(h->stage2);
+    cudaFree(h->partial);
+    cudaFree(h->d_clk);
+    cudaFree(h->d_ctl);
+    for (DevBuf *b : {&h->rain, &h->ev, &h->src_cell, &h->src_q, &h->probe_cells, &h->probe_out}) cudaFree(b->p);
+    if (h->h_clk) cudaFreeHost(h->h_clk);
+    if (h->h_ctl) cudaFreeHost(h->h_ctl);
+    if (h->h_partial) cudaFreeHost(h->h_partial);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return SW2D_OK;
+}
+
+int sw2d_set_static(sw2d_handle *h, const double *z, const double *manning) {
+    if (!h || !z) return fail(h, SW2D_ERR_INVALID_ARG, "z is null");
+    const int rows = h->cfg.rows, cols = h->cfg.cols;
+    const size_t n = (size_t)rows * cols;
+    CK(h, cudaMemcpyAsync(h->stage, z, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    double *dn = nullptr;
+    if (manning) {
+        CK(h, cudaMemcpyAsync(h->stage2, manning, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        dn = h->stage2;
+    }
+    if (is_f64(h))
+        CK(h, launch_pack_static(h->stage, dn, rows, cols, h->pitch, h->cfg.nodata, (double *)h->z,
+                                 dn ? (double *)h->nman : nullptr, h->mask, h->stream));
+    else
+        CK(h, launch_pack_static(h->stage, dn, rows, cols, h->pitch, h->cfg.nodata, (float *)h->z,
+                                 dn ? (float *)h->nman : nullptr, h->mask, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->has_nraster = manning != nullptr;
+    h->have_static = true;
+    h->have_state = false;  // the active mask may have changed
+    h->graph_valid = false;
+    return SW2D_OK;
+}
+
+int sw2d_set_state(sw2d_handle *h, const double *depth, const double *um, const double *vn, double t0) {
+    if (!h || !depth) return fail(h, SW2D_ERR_INVALID_ARG, "depth is null");
+    if (!h->have_static) return fail(h, SW2D_ERR_STATE, "sw2d_set_static must come first");
+    const int rows = h->cfg.rows, cols = h->cfg.cols, pitch = h->pitch;
+    const size_t fb = h->plane * h->real_size;
+    for (int b = 0; b < 2; b++) {
+        CK(h, cudaMemsetAsync(h->h[b], 0, fb, h->stream));
+        CK(h, cudaMemsetAsync(h->um[b], 0, fb, h->stream));
+        CK(h, cudaMemsetAsync(h->vn[b], 0, fb, h->stream));
+    }
+    CK(h, cudaMemcpyAsync(h->stage, depth, (size_t)rows * cols * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (is_f64(h)) CK(h, launch_pack_depth(h->stage, rows, cols, pitch, h->mask, (double *)h->h[0], h->stream));
+    else CK(h, launch_pack_depth(h->stage, rows, cols, pitch, h->mask, (float *)h->h[0], h->stream));
+    const double *su = nullptr, *sv = nullptr;
+    if (um) {
+        CK(h, cudaMemcpyAsync(h->stage, um, (size_t)(rows + 1) * cols * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        su = h->stage;
+    }
+    if (is_f64(h)) CK(h, launch_pack_um(su, rows, cols, pitch, h->G.south_open, h->mask, (double *)h->um[0], h->stream));
+    else CK(h, launch_pack_um(su, rows, cols, pitch, h->G.south_open, h->mask, (float *)h->um[0], h->stream));
+    if (vn) {
+        CK(h, cudaMemcpyAsync(h->stage2, vn, (size_t)rows * (cols + 1) * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        sv = h->stage2;
+    }
+    if (is_f64(h)) CK(h, launch_pack_vn(sv, rows, cols, pitch, h->mask, (double *)h->vn[0], h->stream));
+    else CK(h, launch_pack_vn(sv, rows, cols, pitch, h->mask, (float *)h->vn[0], h->stream));
+    // clock slot 0 = this state; slots 1 and 2 start with empty accumulators
+    Clock c0{};
+    c0.t = t0;
+    c0.buf = 0;
+    CK(h, cudaMemsetAsync(h->d_clk, 0, 3 * sizeof(Clock), h->stream));
+    *h->h_clk = c0;
+    CK(h, cudaMemcpyAsync(h->d_clk, h->h_clk, sizeof(Clock), cudaMemcpyHostToDevice, h->stream));
+    if (is_f64(h))
+        CK(h, launch_cmax((const double *)h->h[0], (const double *)h->um[0], (const double *)h->vn[0], h->mask, rows,
+                          cols, pitch, h->G.south_open, make_thr<double>(h->cfg).ge_th, h->cfg.g,
+                          &h->d_clk[0].cmax_bits, h->stream));
+    else
+        CK(h, launch_cmax((const float *)h->h[0], (const float *)h->um[0], (const float *)h->vn[0], h->mask, rows,
+                          cols, pitch, h->G.south_open, make_thr<float>(h->cfg).ge_th, h->cfg.g,
+                          &h->d_clk[0].cmax_bits, h->stream));
+    h->launches = 0;
+    h->have_state = true;
+    int rc = read_clock(h);
+    if (rc) return rc;
+    sw2d_budget b;
+    rc = sw2d_get_budget(h, &b);
+    if (rc) return rc;
+    h->volume0 = b.volume;
+    return SW2D_OK;
+}
+
+int sw2d_set_rain(sw2d_handle *h, int32_t kind, const double *series, int32_t n, double dt_series) {
+    if (!h) return SW2D_ERR_INVALID_ARG;
+    if (kind == SW2D_RAIN_NONE) {
+        h->F.rain_kind = RAIN_NONE;
+        h->graph_valid = false;
+        return SW2D_OK;
+    }
+    if (kind != SW2D_RAIN_COMPAT && kind != SW2D_RAIN_STEP && kind != SW2D_RAIN_LINEAR)
+        return fail(h, SW2D_ERR_INVALID_ARG, "rain kind must be NONE, COMPAT, STEP or LINEAR (storm: sw2d_set_storm)");
+    if (!series || n < 1 || !(dt_series > 0)) return fail(h, SW2D_ERR_INVALID_ARG, "bad rain series");
+    int rc = upload_table(h, h->rain, series, (size_t)n);
+    if (rc) return rc;
+    h->F.rain_kind = kind;
+    h->F.rain = (const double *)h->rain.p;
+    h->F.n_rain = n;
+    h->F.rain_dt = dt_series;
+    h->graph_valid = false;
+    return SW2D_OK;
+}
+
+int sw2d_set_storm(sw2d_handle *h, double peak, double x0, double y0, double vx, double vy, double sigma,
+                   double t_stop) {
+    if (!h) return SW2D_ERR_INVALID_ARG;
+    if (!(sigma > 0) || !(peak >= 0)) return fail(h, SW2D_ERR_INVALID_ARG, "storm needs sigma > 0 and peak >= 0");
+    h->F.rain_kind = RAIN_STORM;
+    h->F.storm_peak = peak;
+    h->F.storm_x0 = x0;
+    h->F.storm_y0 = y0;
+    h->F.storm_vx = vx;
+    h->F.storm_vy = vy;
+    h->F.storm_sigma = sigma;
+    h->F.storm_tstop = t_stop;
+    h->graph_valid = false;
+    return SW2D_OK;
+}
+
+int sw2d_set_evaporation(sw2d_handle *h, const double *series, int32_t n, double dt_series) {
+    if (!h) return SW2D_ERR_INVALID_ARG;
+    if (n <= 0) {
+        h->F.n_ev = 0;
+        h->graph_valid = false;
+        return SW2D_OK;
+    }
+    if (!series || !(dt_series > 0)) return fail(h, SW2D_ERR_INVALID_ARG, "bad evaporation series");
+    int rc = upload_table(h, h->ev, series, (size_t)n);
+    if (rc) return rc;
+    h->F.ev = (const double *)h->ev.p;
+    h->F.n_ev = n;
+    h->F.ev_dt = dt_series;
+    h->graph_valid = false;
+    return SW2D_OK;
+}
+
+int sw2d_set_point_sources(sw2d_handle *h, const int32_t *cells, int32_t n_src, const double *q, int32_t n_rec,
+                           double dtoq) {
+    if (!h) return SW2D_ERR_INVALID_ARG;
+    if (n_src <= 0) {
+        h->G.n_src = 0;
+        h->graph_valid = false;
+        return SW2D_OK;
+    }
+    if (!cells || !q || n_rec < 1 || !(dtoq > 0)) return fail(h, SW2D_ERR_INVALID_ARG, "bad point-source table");
+    const long long ncell = (long long)h->cfg.rows * h->cfg.cols;
+    for (int s = 0; s < n_src; s++)
+        if (cells[s] < 0 || cells[s] >= ncell) return fail(h, SW2D_ERR_INVALID_ARG, "source cell out of range");
+    int rc = upload_table(h, h->src_cell, cells, (size_t)n_src);
+    if (rc) return rc;
+    rc = upload_table(h, h->src_q, q, (size_t)n_src * n_rec);
+    if (rc) return rc;
+    h->F.src_cell = (const int *)h->src_cell.p;
+    h->F.src_q = (const double *)h->src_q.p;
+    h->F.n_qrec = n_rec;
+    h->F.dtoq = dtoq;
+    h->G.n_src = n_src;
+    h->graph_valid = false;
+    return SW2D_OK;
+}
+
+int sw2d_advance(sw2d_handle *h, int64_t max_steps, double t_end, int64_t *steps_done) {
+    if (steps_done) *steps_done = 0;
+    if (!h) return SW2D_ERR_INVALID_ARG;
+    if (!h->have_static || !h->have_state) return fail(h, SW2D_ERR_STATE, "set_static and set_state must come first");
+    if (max_steps < 0) return fail(h, SW2D_ERR_INVALID_ARG, "max_steps < 0");
+    if (std::isnan(t_end)) return fail(h, SW2D_ERR_INVALID_ARG, "t_end is NaN");
+    CK(h, cudaSetDevice(h->cfg.device));
+    const long long start = h->clock.steps;
+    Control ctl;
+    ctl.t_end = t_end;
+    ctl.step_limit = start + max_steps;
+    *h->h_ctl = ctl;
+    CK(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Control), cudaMemcpyHostToDevice, h->stream));
+    for (;;) {
+        double dtn;
+        double cmax;
+        std::memcpy(&cmax, &h->clock.cmax_bits, sizeof(double));
+        if (!decide_step(h->clock.t, cmax, h->clock.steps, ctl, h->G, &dtn)) break;
+        const long long remaining = ctl.step_limit - h->clock.steps;
+        if (remaining >= kChunk) {
+            if (!h->graph_valid) {
+                int rc = capture_graph(h);
+                if (rc) return rc;
+            }
+            CK(h, cudaGraphLaunch(h->graph, h->stream));
+            h->launches += kChunk;
+        } else {
+            const long long n = ((remaining + 2) / 3) * 3;
+            for (long long m = 0; m < n; m++) {
+                CK(h, launch_one(h, (int)((h->launches) % 3)));
+                h->launches++;
+            }
+        }
+        int rc = read_clock(h);
+        if (rc) return rc;
+        if (h->clock.nonfinite) {
+            if (steps_done) *steps_done = h->clock.steps - start;
+            return fail(h, SW2D_ERR_NONFINITE, "a non-finite depth or discharge was produced");
+        }
+        if (h->clock.status & ST_TOO_MANY_LOCAL_SOURCES)
+            return fail(h, SW2D_ERR_INVALID_ARG, "more than 64 point sources fall in one tile");
+        if (!h->clock.ran) break;
+    }
+    if (steps_done) *steps_done = h->clock.steps - start;
+    return SW2D_OK;
+}
+
+int sw2d_get_field(sw2d_handle *h, int32_t field, double *out) {
+    if (!h || !out) return fail(h, SW2D_ERR_INVALID_ARG, "null argument");
+    if (!h->have_state && field != SW2D_FIELD_ELEVATION) return fail(h, SW2D_ERR_STATE, "no state");
+    const int rows = h->cfg.rows, cols = h->cfg.cols, pitch = h->pitch;
+    const int b = h->clock.buf;
+    const bool f64 = is_f64(h);
+    int nr = rows, nc = cols;
+    const void *src = nullptr;
+    switch (field) {
+    case SW2D_FIELD_DEPTH: src = h->h[b]; break;
+    case SW2D_FIELD_UM: src = h->um[b]; nr = rows + 1; break;
+    case SW2D_FIELD_VN: src = h->vn[b]; nc = cols + 1; break;
+    case SW2D_FIELD_ELEVATION: src = h->z; break;
+    case SW2D_FIELD_UU:
+    case SW2D_FIELD_VV: {
+        if (f64)
+            CK(h, launch_velocity((const double *)h->h[b], (const double *)h->um[b], (const double *)h->vn[b], rows, cols,
+                                  pitch, make_thr<double>(h->cfg).ge_th, h->stage, h->stage2, h->stream));
+        else
+            CK(h, launch_velocity((const float *)h->h[b], (const float *)h->um[b], (const float *)h->vn[b], rows, cols,
+                                  pitch, make_thr<float>(h->cfg).ge_th, h->stage, h->stage2, h->stream));
+        const double *s = field == SW2D_FIELD_UU ? h->stage : h->stage2;
+        CK(h, cudaMemcpyAsync(out, s, (size_t)rows * cols * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        return SW2D_OK;
+    }
+    default:
+        return fail(h, SW2D_ERR_INVALID_ARG, "unknown field");
+    }
+    if (f64) CK(h, launch_unpack((const double *)src, nr, nc, pitch, h->stage, h->stream));
+    else CK(h, launch_unpack((const float *)src, nr, nc, pitch, h->stage, h->stream));
+    CK(h, cudaMemcpyAsync(out, h->stage, (size_t)nr * nc * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return SW2D_OK;
+}
+
+int sw2d_get_budget(sw2d_handle *h, sw2d_budget *out) {
+    if (!h || !out) return fail(h, SW2D_ERR_INVALID_ARG, "null argument");
+    if (!h->have_state) return fail(h, SW2D_ERR_STATE, "no state");
+    const int b = h->clock.buf;
+    if (is_f64(h))
+        CK(h, launch_volume((const double *)h->h[b], h->mask, h->cfg.rows, h->cfg.cols, h->pitch, h->partial,
+                            kVolumeBlocks, h->stream));
+    else
+        CK(h, launch_volume((const float *)h->h[b], h->mask, h->cfg.rows, h->cfg.cols, h->pitch, h->partial,
+                            kVolumeBlocks, h->stream));
+    CK(h, cudaMemcpyAsync(h->h_partial, h->partial, kVolumeBlocks * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    double s = 0.0, c = 0.0;
+    for (int k = 0; k < kVolumeBlocks; k++) {
+        double y = h->h_partial[k] - c;
+        double t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    const Clock &k = h->clock;
+    double tot[B_N];
+    for (int q = 0; q < B_N; q++) {  // fold the last iteration's sums
+        double y = k.step[q] - k.tot_c[q];
+        tot[q] = k.tot_s[q] + y;
+    }
+    std::memset(out, 0, sizeof(*out));
+    out->t = k.t;
+    out->dt = k.dt;
+    std::memcpy(&out->cmax, &k.cmax_bits, sizeof(double));
+    out->volume = s * h->cfg.dx * h->cfg.dy;
+    out->volume0 = h->volume0;
+    out->rain_in = tot[B_RAIN];
+    out->source_in = tot[B_SRC];
+    out->evap_out = tot[B_EV];
+    out->outflow = tot[B_OUT];
+    out->clamp_gain = tot[B_CLAMP];
+    out->steps = k.steps;
+    out->nonfinite = k.nonfinite ? 1 : 0;
+    return SW2D_OK;
+}
+
+int sw2d_probe(sw2d_handle *h, const int32_t *cells, int32_t n, double *out) {
+    if (!h || (n > 0 && (!cells || !out))) return fail(h, SW2D_ERR_INVALID_ARG, "null argument");
+    if (!h->have_state) return fail(h, SW2D_ERR_STATE, "no state");
+    if (n <= 0) return SW2D_OK;
+    int rc = upload_table(h, h->probe_cells, cells, (size_t)n);
+    if (rc) return rc;
+    if (h->probe_out.bytes < (size_t)n * sizeof(double)) {
+        cudaFree(h->probe_out.p);
+        h->probe_out.p = nullptr;
+        h->probe_out.bytes = 0;
+        CK(h, cudaMalloc(&h->probe_out.p, (size_t)n * sizeof(double)));
+        h->probe_out.bytes = (size_t)n * sizeof(double);
+    }
+    const int b = h->clock.buf;
+    if (is_f64(h))
+        CK(h, launch_probe((const double *)h->h[b], h->cfg.rows, h->cfg.cols, h->pitch, (const int *)h->probe_cells.p, n,
+                           (double *)h->probe_out.p, h->stream));
+    else
+        CK(h, launch_probe((const float *)h->h[b], h->cfg.rows, h->cfg.cols, h->pitch, (const int *)h->probe_cells.p, n,
+                           (double *)h->probe_out.p, h->stream));
+    CK(h, cudaMemcpyAsync(out, h->probe_out.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return SW2D_OK;
+}
+
+int sw2d_synchronize(sw2d_handle *h) {
+    if (!h) return SW2D_ERR_INVALID_ARG;
+    CK(h, cudaStreamSynchronize(h->stream));
+    return SW2D_OK;
+}
+
+int sw2d_get_stream(sw2d_handle *h, void **stream) {
+    if (!h || !stream) return SW2D_ERR_INVALID_ARG;
+    *stream = (void *)h->stream;
+    return SW2D_OK;
+}
+
+int sw2d_launch_count(sw2d_handle *h, int64_t *launches) {
+    if (!h || !launches) return SW2D_ERR_INVALID_ARG;
+    *launches = h->launches;
+    return SW2D_OK;
+}
+
+const char *sw2d_last_error(const sw2d_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+const char *sw2d_status_string(int32_t s) {
+    switch (s) {
+    case SW2D_OK: return "ok";
+    case SW2D_ERR_INVALID_ARG: return "invalid argument";
+    case SW2D_ERR_OOM: return "out of device memory";
+    case SW2D_ERR_CUDA: return "CUDA error";
+    case SW2D_ERR_NONFINITE: return "non-finite value produced";
+    case SW2D_ERR_TIMEOUT: return "device-side wait timed out";
+    case SW2D_ERR_STATE: return "call order";
+    default: return "unknown status";
+    }
+}
+
+}  // extern "C"

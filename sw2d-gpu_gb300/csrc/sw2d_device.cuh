@@ -1,0 +1,701 @@
+// sw2d_device.cuh -- device-side types and the fused step kernel.
+//
+// One launch of step_kernel advances the whole domain by one iteration of
+// the reference solver loop (SW2D-GPU_linux/src/SW2D-GPU.cu:1256-1336,
+// "cu:<line>" below).  The reference runs that iteration as nine kernels
+// with a host synchronisation after each and re-reads/re-writes 20 FP64
+// arrays; here one CTA owns a TH x TW tile of cells, stages the tile plus a
+// halo of 4 cells (north/west) and 3 cells (south/east) in shared memory
+// and performs, entirely on chip:
+//
+//   stage 1  face depths hm/hn and face velocities uu1/vv1   (cu:363-453)
+//   stage 2  new face discharges um/vn, momentum + dry bed   (cu:98-354)
+//   stage 3  provisional depth h*, forcing at t              (cu:603-665)
+//   stage 4  dry-cell outflow fix on each face (cu:695-725) and the final
+//            depth, forcing at t+dt                           (cu:603-665)
+//   stage 5  wave-speed bound of the new state (CFL rule, extension) and
+//            the FP64 budget partials
+//
+// The transverse averages uua/vva (cu:490-523) are formed on the fly from
+// uu1/vv1 in shared memory.  Only the state (h, um, vn) lives in HBM, in two
+// ping-pong buffers; static fields (z, Manning n, active mask) are read-only.
+//
+// The dependency radius of one iteration is 3 cells (momentum needs h at
+// i-2..i+1, the provisional depth needs the four new faces, the fix needs
+// the provisional depth of both cells of a face).  One extra ring on the
+// north/west sides gives the final depth of the neighbours of every owned
+// face, so that the CFL bound of the NEW state is known when the launch
+// ends and the next launch can pick its time step without a grid-wide
+// synchronisation.
+//
+// The same template serves FP64 (compiled without FMA contraction, so that
+// every operation rounds exactly as in the serial oracle and the reference
+// built with --fmad=false) and FP32 (fast math).  Threshold tests are
+// written as `x >= c` against host-computed constants so that the FP32 path
+// decides wet/dry exactly as an FP64 comparison with th = 1e-4 would.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sw2d {
+
+enum { B_RAIN = 0, B_SRC = 1, B_EV = 2, B_OUT = 3, B_CLAMP = 4, B_N = 5 };
+
+enum { ST_TOO_MANY_LOCAL_SOURCES = 1 };
+
+constexpr int kMaxLocalSources = 64;
+
+// Per-iteration bookkeeping.  Three slots rotate: launch m reads slot m%3,
+// writes slot (m+1)%3 and clears the accumulators of slot (m+2)%3, which is
+// the one launch m+1 will write.  So no launch ever reads a slot that a
+// concurrent CTA is still accumulating into.
+struct __align__(16) Clock {
+    double t;                      // time at the start of the next iteration
+    double dt;                     // half step of the last iteration
+    unsigned long long cmax_bits;  // CFL speed bound of this state (atomicMax on bits)
+    long long steps;               // iterations since set_state
+    int buf;                       // ping-pong buffer holding this state
+    int ran;                       // the launch that wrote this slot advanced the state
+    unsigned int nonfinite;        // a non-finite value was produced (sticky)
+    unsigned int status;           // device-side error bits (sticky)
+    double tot_s[B_N], tot_c[B_N]; // Kahan running totals of the budgets [m^3]
+    double step[B_N];              // budget sums of the iteration that wrote this slot
+};
+
+struct Control {
+    double t_end;
+    long long step_limit;
+};
+
+struct GridDesc {
+    int rows, cols, pitch, tiles_w;
+    int dt_mode, south_open, n_src, pad0;
+    double dx, dy, g, th, cfl, dmin, dt_half;
+    double pct_hi, pct_lo;  // 1 - LWL and 1 - (INT + INF)   (cu:627-634)
+    double manning;
+};
+
+struct ForcingDesc {
+    int rain_kind, n_rain, n_ev, n_qrec;
+    const double *rain;
+    double rain_dt;
+    double storm_peak, storm_x0, storm_y0, storm_vx, storm_vy, storm_sigma, storm_tstop;
+    const double *ev;
+    double ev_dt;
+    const int *src_cell;
+    const double *src_q;
+    double dtoq;
+};
+
+template <class Real>
+struct StateBufs {
+    Real *h[2];
+    Real *um[2];
+    Real *vn[2];
+    const Real *z;
+    const Real *nman;  // per-cell Manning n or nullptr
+    const uint8_t *mask;
+};
+
+// wet/dry thresholds as `x >= c` constants (see file comment)
+template <class Real>
+struct Thr {
+    Real gt_th;     // x > th      <=>  x >= gt_th
+    Real ge_th;     // x >= th     <=>  x >= ge_th
+    Real gt_evmin;  // x > EV_WL_min
+};
+
+enum { RAIN_NONE = 0, RAIN_COMPAT = 1, RAIN_STEP = 2, RAIN_LINEAR = 3, RAIN_STORM = 4 };
+
+// ---------------------------------------------------------------------------
+// time step decision, shared by host and device (one definition, so the host
+// loop and every CTA decide identically)
+// ---------------------------------------------------------------------------
+__host__ __device__ inline bool decide_step(double t, double cmax, long long steps,
+                                            const Control &ctl, const GridDesc &G,
+                                            double *dt_half) {
+    if (steps >= ctl.step_limit) return false;
+    if (G.dt_mode == 0) {
+        if (!(t + G.dt_half <= ctl.t_end)) return false;  // cu:1256
+        *dt_half = G.dt_half;
+        return true;
+    }
+    if (!(ctl.t_end - t > 1.0e-9)) return false;
+    double dt2 = 2.0 * G.dt_half;
+    if (cmax > 0.0) {
+        double cand = G.cfl * G.dmin / cmax;
+        if (cand < dt2) dt2 = cand;
+    }
+    if (t + dt2 > ctl.t_end) dt2 = ctl.t_end - t;
+    *dt_half = 0.5 * dt2;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// forcing (stream_flow cu:526-555, evaporation_load cu:589-601)
+// ---------------------------------------------------------------------------
+__device__ inline double compat_series(const double *v, int n, double dtv, double t) {
+    if (n <= 0) return 0.0;
+    if (t <= 1.00) return v[0] * t;
+    int it = (int)(t / dtv);
+    int a = it < n ? it : n - 1;
+    int b = it + 1 < n ? it + 1 : n - 1;
+    return v[a] + (v[b] - v[a]) / (dtv * (t - dtv * (it)));
+}
+
+__device__ inline double rain_uniform(const ForcingDesc &F, double t) {
+    switch (F.rain_kind) {
+    case RAIN_COMPAT:
+        return compat_series(F.rain, F.n_rain, F.rain_dt, t) / (F.rain_dt * 1000.0);
+    case RAIN_STEP: {
+        if (t < 0.0) return 0.0;
+        long long k = (long long)floor(t / F.rain_dt);
+        if (k >= F.n_rain) return 0.0;
+        return F.rain[k] / 3.6e6;
+    }
+    case RAIN_LINEAR: {
+        if (t < 0.0 || F.n_rain < 2) return 0.0;
+        double s = t / F.rain_dt;
+        long long k = (long long)floor(s);
+        if (k >= F.n_rain - 1) return 0.0;
+        double w = s - (double)k;
+        return (F.rain[k] + w * (F.rain[k + 1] - F.rain[k])) / 3.6e6;
+    }
+    default:
+        return 0.0;
+    }
+}
+
+__device__ inline double evap_rate(const ForcingDesc &F, double t) {
+    if (F.n_ev <= 0) return 0.0;
+    return compat_series(F.ev, F.n_ev, F.ev_dt, t) / (F.ev_dt * 1000.0);
+}
+
+__device__ inline double source_rate(const ForcingDesc &F, int n_src, int s, double t, double area) {
+    double q;
+    if (t <= 1.00) {
+        q = F.src_q[s] * t;
+    } else {
+        int it = (int)(t / F.dtoq);
+        int a = it < F.n_qrec ? it : F.n_qrec - 1;
+        int b = it + 1 < F.n_qrec ? it + 1 : F.n_qrec - 1;
+        double qa = F.src_q[(size_t)a * n_src + s];
+        double qb = F.src_q[(size_t)b * n_src + s];
+        q = qa + (qb - qa) / (F.dtoq * (t - F.dtoq * (it)));
+    }
+    return q / area;
+}
+
+// ---------------------------------------------------------------------------
+// precision traits
+// ---------------------------------------------------------------------------
+template <class Real>
+struct RT;
+
+template <>
+struct RT<double> {
+    static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+    static __device__ __forceinline__ double pow_(double x) { return pow(x, 1.3333330); }  // cu:195
+    static __device__ __forceinline__ double exp_(double x) { return exp(x); }
+    static __device__ __forceinline__ bool finite_(double x) { return isfinite(x); }
+};
+
+template <>
+struct RT<float> {
+    static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+    static __device__ __forceinline__ float pow_(float x) { return __powf(x, 1.3333330f); }
+    static __device__ __forceinline__ float exp_(float x) { return __expf(x); }
+    static __device__ __forceinline__ bool finite_(float x) { return isfinite(x); }
+};
+
+// Dry-bed rules (cu:130-159 / cu:247-276).  `a` is the low-index cell of the
+// face (north / west), `b` the high-index cell.  Returns true and sets q
+// when a rule applies; false means "use the momentum equation".
+template <class Real>
+__device__ __forceinline__ bool dry_bed(const Thr<Real> &T, Real g, Real ha, Real za, Real hb,
+                                        Real zb, Real &q) {
+    if (hb + zb < za) {  // cu:130
+        q = (ha >= T.gt_th) ? Real(0.5440) * ha * RT<Real>::sqrt_(g * ha) : Real(0);
+        return true;
+    }
+    if (ha + za < zb) {  // cu:138
+        q = (hb >= T.gt_th) ? Real(-0.544) * hb * RT<Real>::sqrt_(g * hb) : Real(0);
+        return true;
+    }
+    // cu:149: (hb - th) * (ha - th) < 0, i.e. exactly one side strictly wet
+    const bool b_wet = hb >= T.gt_th, a_wet = ha >= T.gt_th;
+    const bool b_dry = !(hb >= T.ge_th), a_dry = !(ha >= T.ge_th);
+    if ((b_wet && a_dry) || (b_dry && a_wet)) {
+        if ((hb > Real(0)) || (ha > Real(0))) {
+            // -sgn(hb - ha) * 0.350 with sgn from the wet side (cu:151-154)
+            const Real s = b_wet ? Real(-0.350) : Real(0.350);
+            const Real ea = ha + za, eb = hb + zb;
+            const Real hh3 = fmax(eb, ea) - fmax(zb, za);
+            q = s * hh3 * RT<Real>::sqrt_(Real(2.00) * g * hh3);
+        } else {
+            q = Real(0);
+        }
+        return true;
+    }
+    return false;
+}
+
+// upwinded flux through one side of a control volume (pattern of cu:174)
+template <class Real>
+__device__ __forceinline__ Real upwind(Real vel, Real q_other, Real q_self) {
+    return vel * (q_other + q_self) * Real(0.50) + fabs(vel) * (q_self - q_other) * Real(0.50);
+}
+template <class Real>
+__device__ __forceinline__ Real upwind_r(Real vel, Real q_other, Real q_self) {
+    // same with the operand order of the "left"/"down" sides (cu:175, cu:188)
+    return vel * (q_self + q_other) * Real(0.50) + fabs(vel) * (q_other - q_self) * Real(0.50);
+}
+
+// ---------------------------------------------------------------------------
+// the fused step kernel
+// ---------------------------------------------------------------------------
+template <class Real, int TH, int TW>
+constexpr size_t step_smem_bytes() {
+    return (size_t)(TH + 7) * (TW + 7) * (10 * sizeof(Real) + 1) + 64;
+}
+
+template <class Real, int TH, int TW, int NT>
+__global__ void __launch_bounds__(NT)
+    step_kernel(const GridDesc G, const ForcingDesc F, const StateBufs<Real> S, const Thr<Real> T,
+                Clock *__restrict__ clk, const Control *__restrict__ ctl, const int slot) {
+    constexpr int HN = 4;                       // halo north/west (3 + CFL ring)
+    constexpr int RH = TH + 7, RW = TW + 7, RN = RH * RW;
+    constexpr int NW = NT / 32;
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Real *s_h = reinterpret_cast<Real *>(smem_raw);
+    Real *s_z = s_h + RN;
+    Real *s_umo = s_z + RN;  // old um, later the corrected new um
+    Real *s_vno = s_umo + RN;
+    Real *s_uu1 = s_vno + RN;
+    Real *s_vv1 = s_uu1 + RN;
+    Real *s_rum = s_vv1 + RN;  // new um before the dry-cell fix
+    Real *s_rvn = s_rum + RN;
+    Real *s_hs = s_rvn + RN;   // provisional depth
+    Real *s_n = s_hs + RN;     // Manning n per cell (only if G has a raster)
+    uint8_t *s_m = reinterpret_cast<uint8_t *>(s_n + RN);
+
+    __shared__ double s_red[NW][B_N + 1];
+    __shared__ int s_nloc;
+    __shared__ int s_srcp[kMaxLocalSources];
+    __shared__ Real s_srcq0[kMaxLocalSources], s_srcq1[kMaxLocalSources];
+    __shared__ int s_wcnt[NW];
+    __shared__ double s_f[4];  // rain(t), rain(t+dt), evap(t), evap(t+dt)
+
+    const int tid = threadIdx.x;
+    const int slot_out = slot == 2 ? 0 : slot + 1;
+    const int slot_nx = slot == 0 ? 2 : slot - 1;
+    const Clock &ci = clk[slot];
+    const double t0 = ci.t;
+    double dt = 0.0;
+    const bool run = decide_step(t0, __longlong_as_double((long long)ci.cmax_bits), ci.steps, *ctl, G, &dt);
+
+    if (blockIdx.x == 0 && tid == 0) {
+        Clock &co = clk[slot_out];
+        for (int k = 0; k < B_N; k++) {  // fold the previous iteration's sums (Kahan)
+            double s = ci.tot_s[k], c = ci.tot_c[k];
+            double y = ci.step[k] - c;
+            double tt = s + y;
+            co.tot_c[k] = (tt - s) - y;
+            co.tot_s[k] = tt;
+        }
+        co.t = run ? (t0 + dt) + dt : t0;  // cu:1297, cu:1335
+        co.dt = run ? dt : ci.dt;
+        co.steps = ci.steps + (run ? 1 : 0);
+        co.buf = run ? 1 - ci.buf : ci.buf;
+        co.ran = run ? 1 : 0;
+        if (!run) co.cmax_bits = ci.cmax_bits;
+        atomicOr(&co.nonfinite, ci.nonfinite);
+        atomicOr(&co.status, ci.status);
+        Clock &cn = clk[slot_nx];
+        cn.cmax_bits = 0ull;
+        cn.nonfinite = 0u;
+        cn.status = 0u;
+        for (int k = 0; k < B_N; k++) cn.step[k] = 0.0;
+    }
+    if (!run) return;
+
+    const int rows = G.rows, cols = G.cols, pitch = G.pitch;
+    const int ti = blockIdx.x / G.tiles_w, tj = blockIdx.x - ti * G.tiles_w;
+    const int I0 = ti * TH - HN, J0 = tj * TW - HN;  // global index of smem (0,0)
+    const int buf = ci.buf;
+    const Real *__restrict__ Hin = S.h[buf];
+    const Real *__restrict__ Uin = S.um[buf];
+    const Real *__restrict__ Vin = S.vn[buf];
+    Real *__restrict__ Hout = S.h[1 - buf];
+    Real *__restrict__ Uout = S.um[1 - buf];
+    Real *__restrict__ Vout = S.vn[1 - buf];
+    const bool has_n = S.nman != nullptr;
+
+    const double t1 = t0 + dt;  // time of the second continuity call (cu:1297)
+    const double dt2d = 2.00 * dt;  // cu:808
+    const Real dt2 = (Real)dt2d;
+    const Real dx = (Real)G.dx, dy = (Real)G.dy, g = (Real)G.g;
+    const Real dt2dx = (Real)(dt2d / G.dx), dt2dy = (Real)(dt2d / G.dy);
+    const Real manning = (Real)G.manning;
+
+    // ---- stage 0: stage the tile + halo in shared memory --------------------
+    for (int idx = tid; idx < RN; idx += NT) {
+        const int r = idx / RW, c = idx - (idx / RW) * RW;
+        const int gi = I0 + r, gj = J0 + c;
+        const bool in_r = (unsigned)gi < (unsigned)rows, in_c = (unsigned)gj < (unsigned)cols;
+        const size_t gp = (size_t)gi * pitch + gj;
+        Real hv = 0, zv = 0, nv = 0;
+        uint8_t mv = 0;
+        if (in_r && in_c) {
+            hv = Hin[gp];
+            zv = S.z[gp];
+            mv = S.mask[gp];
+            if (has_n) nv = S.nman[gp];
+        }
+        s_h[idx] = hv;
+        s_z[idx] = zv;
+        s_m[idx] = mv;
+        if (has_n) s_n[idx] = nv;
+        s_umo[idx] = ((unsigned)gi <= (unsigned)rows && in_c) ? Uin[gp] : Real(0);
+        s_vno[idx] = (in_r && (unsigned)gj <= (unsigned)cols) ? Vin[gp] : Real(0);
+    }
+    if (tid == 0) {
+        s_f[0] = rain_uniform(F, t0);
+        s_f[1] = rain_uniform(F, t1);
+        s_f[2] = evap_rate(F, t0);
+        s_f[3] = evap_rate(F, t1);
+        s_nloc = 0;
+    }
+    // point sources inside this tile's provisional-depth region, kept in
+    // list order so that a later source on the same cell wins (cu:545)
+    if (G.n_src > 0) {
+        __syncthreads();
+        const double area = G.dx * G.dy;
+        for (int base = 0; base < G.n_src; base += NT) {
+            const int s = base + tid;
+            bool in = false;
+            int p = 0;
+            if (s < G.n_src) {
+                const int cell = F.src_cell[s];
+                const int gi = cell / cols, gj = cell - (cell / cols) * cols;
+                const int r = gi - I0, c = gj - J0;
+                in = (r >= 2 && r < TH + 5 && c >= 2 && c < TW + 5);
+                p = r * RW + c;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, in);
+            const int lane = tid & 31, wid = tid >> 5;
+            if (lane == 0) s_wcnt[wid] = __popc(bal);
+            __syncthreads();
+            if (in) {
+                int off = s_nloc;
+                for (int w = 0; w < wid; w++) off += s_wcnt[w];
+                off += __popc(bal & ((1u << lane) - 1u));
+                if (off < kMaxLocalSources) {
+                    s_srcp[off] = p;
+                    s_srcq0[off] = (Real)source_rate(F, G.n_src, s, t0, area);
+                    s_srcq1[off] = (Real)source_rate(F, G.n_src, s, t1, area);
+                } else {
+                    atomicOr(&clk[slot_out].status, (unsigned)ST_TOO_MANY_LOCAL_SOURCES);
+                }
+            }
+            __syncthreads();
+            if (tid == 0) {
+                int tot = s_nloc;
+                for (int w = 0; w < NW; w++) tot += s_wcnt[w];
+                s_nloc = tot < kMaxLocalSources ? tot : kMaxLocalSources;
+            }
+            __syncthreads();  // s_wcnt is rewritten by the next chunk
+        }
+    }
+    __syncthreads();
+
+    const Real rr0_u = (Real)s_f[0], rr1_u = (Real)s_f[1];
+    const Real ev0 = (Real)s_f[2], ev1 = (Real)s_f[3];
+    const int nloc = s_nloc;
+    const Real pct_hi = (Real)G.pct_hi, pct_lo = (Real)G.pct_lo;
+    const bool storm = F.rain_kind == RAIN_STORM;
+
+    // ---- stage 1: face depths and velocities (cu:363-453) ------------------
+    for (int idx = tid; idx < RN; idx += NT) {
+        const int r = idx / RW, c = idx - (idx / RW) * RW;
+        const int gi = I0 + r, gj = J0 + c;
+        if (r >= 1) {
+            Real hm;
+            if (gi == rows) hm = s_h[idx - RW];
+            else if (gi == 0) hm = s_h[idx];
+            else hm = Real(0.50) * (s_h[idx] + s_h[idx - RW]);
+            s_uu1[idx] = (hm >= T.ge_th) ? s_umo[idx] / hm : Real(0.00);
+        }
+        if (c >= 1) {
+            Real hn;
+            if (gj == cols) hn = s_h[idx - 1];
+            else if (gj == 0) hn = s_h[idx];
+            else hn = Real(0.50) * (s_h[idx] + s_h[idx - 1]);
+            s_vv1[idx] = (hn >= T.ge_th) ? s_vno[idx] / hn : Real(0.0);
+        }
+    }
+    __syncthreads();
+
+    // ---- stage 2: new face discharges (cu:98-354) ---------------------------
+    constexpr int FH = TH + 4, FW = TW + 4;  // rows/cols [2, TH+6) x [2, TW+6)
+    for (int k = tid; k < FH * FW; k += NT) {
+        const int r = 2 + k / FW, c = 2 + (k - (k / FW) * FW);
+        const int p = r * RW + c;
+        const int gi = I0 + r, gj = J0 + c;
+        // x-face (gi, gj): between cells (gi-1, gj) "a" and (gi, gj) "b"
+        Real qx = 0;
+        if ((unsigned)gj < (unsigned)cols) {
+            if (gi > 0 && gi < rows) {
+                const int pa = p - RW;
+                const Real hb = s_h[p], ha = s_h[pa];
+                if (s_m[p] && s_m[pa] && ((ha >= T.gt_th) || (hb >= T.gt_th))) {
+                    const Real zb = s_z[p], za = s_z[pa];
+                    if (!dry_bed<Real>(T, g, ha, za, hb, zb, qx)) {
+                        const Real hm = Real(0.50) * (hb + ha);
+                        const Real u13 = g * hm * dt2dx * (hb + zb - ha - za);  // cu:166
+                        const Real uu_s = s_uu1[p + RW], uu_c = s_uu1[p], uu_n = s_uu1[pa];
+                        const Real mo_s = s_umo[p + RW], mo_c = s_umo[p], mo_n = s_umo[pa];
+                        const Real u11uur = Real(0.50) * (uu_s + uu_c);
+                        const Real u11uul = Real(0.50) * (uu_c + uu_n);
+                        const Real umr = upwind<Real>(u11uur, mo_s, mo_c);
+                        const Real uml = upwind_r<Real>(u11uul, mo_n, mo_c);
+                        const Real u11 = dt2dx * (umr - uml);  // cu:176
+                        Real u12;
+                        if (gj == 0) {
+                            u12 = 0;  // cu:178-180
+                        } else {
+                            const Real u12vvu = Real(0.50) * (s_vv1[p + 1] + s_vv1[pa + 1]);
+                            const Real u12vvd = Real(0.50) * (s_vv1[p] + s_vv1[pa]);
+                            const Real umu = upwind<Real>(u12vvu, s_umo[p + 1], mo_c);
+                            const Real umd = upwind_r<Real>(u12vvd, s_umo[p - 1], mo_c);
+                            u12 = dt2dy * (umu - umd);  // cu:189
+                        }
+                        const Real rn = has_n ? Real(0.5) * (s_n[p] + s_n[pa]) : manning;
+                        Real ram = 0;
+                        if ((hm >= T.gt_th) && rn != Real(0)) {  // cu:194-199
+                            const Real vva = Real(0.250) * (s_vv1[p] + s_vv1[p + 1] + s_vv1[pa] + s_vv1[pa + 1]);
+                            const Real sqx = RT<Real>::sqrt_(uu_c * uu_c + vva * vva);
+                            ram = g * rn * rn * sqx / RT<Real>::pow_(hm);
+                        }
+                        qx = ((Real(1.00) - dt2 * ram * Real(0.50)) * mo_c + (-u11 - u12 - u13)) /
+                             (Real(1.00) + dt2 * ram * Real(0.50));  // cu:203
+                    }
+                }
+            } else if (gi == rows && G.south_open) {
+                const int pa = p - RW;
+                const Real ha = s_h[pa];
+                qx = (s_m[pa] && ha >= T.gt_th) ? Real(0.5440) * ha * RT<Real>::sqrt_(g * ha) : Real(0);
+            }
+        }
+        s_rum[p] = qx;
+        // y-face (gi, gj): between cells (gi, gj-1) "a" and (gi, gj) "b"
+        Real qy = 0;
+        if ((unsigned)gi < (unsigned)rows && gj > 0 && gj < cols) {
+            const int pa = p - 1;
+            const Real hb = s_h[p], ha = s_h[pa];
+            if (s_m[p] && s_m[pa] && ((ha >= T.gt_th) || (hb >= T.gt_th))) {
+                const Real zb = s_z[p], za = s_z[pa];
+                if (!dry_bed<Real>(T, g, ha, za, hb, zb, qy)) {
+                    const Real hn = Real(0.50) * (hb + ha);
+                    const Real v13 = g * hn * dt2dy * (hb + zb - ha - za);  // cu:283
+                    const Real mo_c = s_vno[p];
+                    Real v11;
+                    if (gi == 0) {
+                        v11 = 0;  // cu:289-291
+                    } else {
+                        const Real v11uur = Real(0.50) * (s_uu1[p + RW] + s_uu1[p + RW - 1]);
+                        const Real v11uul = Real(0.50) * (s_uu1[p] + s_uu1[p - 1]);
+                        const Real vnr = upwind<Real>(v11uur, s_vno[p + RW], mo_c);
+                        const Real vnl = upwind_r<Real>(v11uul, s_vno[p - RW], mo_c);
+                        v11 = dt2dx * (vnr - vnl);  // cu:300
+                    }
+                    const Real vv_c = s_vv1[p];
+                    const Real v12vvu = Real(0.50) * (s_vv1[p + 1] + vv_c);
+                    const Real v12vvd = Real(0.50) * (vv_c + s_vv1[p - 1]);
+                    const Real vnu = upwind<Real>(v12vvu, s_vno[p + 1], mo_c);
+                    const Real vnd = upwind_r<Real>(v12vvd, s_vno[p - 1], mo_c);
+                    const Real v12 = dt2dy * (vnu - vnd);  // cu:307
+                    const Real rn = has_n ? Real(0.5) * (s_n[p] + s_n[pa]) : manning;
+                    Real ram = 0;
+                    if ((hn >= T.gt_th) && rn != Real(0)) {  // cu:311-316
+                        const Real uua = Real(0.250) * (s_uu1[p] + s_uu1[p + RW] + s_uu1[p - 1] + s_uu1[p + RW - 1]);
+                        const Real sqy = RT<Real>::sqrt_(uua * uua + vv_c * vv_c);
+                        ram = g * rn * rn * sqy / RT<Real>::pow_(hn);
+                    }
+                    qy = ((Real(1.00) - dt2 * ram * Real(0.50)) * mo_c + (-v11 - v12 - v13)) /
+                         (Real(1.00) + dt2 * ram * Real(0.50));  // cu:320
+                }
+            }
+        }
+        s_rvn[p] = qy;
+    }
+    __syncthreads();
+
+    // storm rain at a cell centre
+    auto storm_rate = [&](int gi, int gj, double tt) -> Real {
+        if (tt >= F.storm_tstop) return Real(0);
+        const Real xc = (Real)(F.storm_x0 + F.storm_vx * tt);
+        const Real yc = (Real)(F.storm_y0 + F.storm_vy * tt);
+        const Real x = ((Real)gj + Real(0.5)) * dx - xc;
+        const Real y = ((Real)gi + Real(0.5)) * dy - yc;
+        const Real s2 = (Real)F.storm_sigma * (Real)F.storm_sigma;
+        return (Real)(F.storm_peak / 3.6e6) * RT<Real>::exp_(-(x * x + y * y) / (Real(2.0) * s2));
+    };
+
+    // ---- stage 3: provisional depth with forcing at t (cu:1278-1288) -------
+    constexpr int PH = TH + 3, PW = TW + 3;  // rows/cols [2, TH+5) x [2, TW+5)
+    for (int k = tid; k < PH * PW; k += NT) {
+        const int r = 2 + k / PW, c = 2 + (k - (k / PW) * PW);
+        const int p = r * RW + c;
+        Real hv = 0;
+        if (s_m[p]) {
+            const Real ho = s_h[p];
+            const bool hi = ho >= T.gt_evmin;
+            const Real pct = hi ? pct_hi : pct_lo;
+            const Real evapo = hi ? ev0 : Real(0.000);
+            Real ql = 0;
+            for (int q = 0; q < nloc; q++)
+                if (s_srcp[q] == p) ql = s_srcq0[q];
+            const Real rr = storm ? storm_rate(I0 + r, J0 + c, t0) : rr0_u;
+            hv = ho - dt2 * ((s_rum[p + RW] - s_rum[p]) / dx + (s_rvn[p + 1] - s_rvn[p]) / dy - ql - rr * pct + evapo);
+            hv = fmax(hv, Real(0.00));  // cu:657
+        }
+        s_hs[p] = hv;
+    }
+    __syncthreads();
+
+    // ---- stage 4: dry-cell fix per face (cu:695-725) + final depth ----------
+    // corrected x-face at p: zero if it drains a dry cell
+    auto fix_x = [&](int p) -> Real {
+        const Real q = s_rum[p];
+        if (q > Real(0) && s_m[p - RW] && !(s_hs[p - RW] >= T.ge_th)) return Real(0);
+        if (q < Real(0) && s_m[p] && !(s_hs[p] >= T.ge_th)) return Real(0);
+        return q;
+    };
+    auto fix_y = [&](int p) -> Real {
+        const Real q = s_rvn[p];
+        if (q > Real(0) && s_m[p - 1] && !(s_hs[p - 1] >= T.ge_th)) return Real(0);
+        if (q < Real(0) && s_m[p] && !(s_hs[p] >= T.ge_th)) return Real(0);
+        return q;
+    };
+
+    // per-thread partials in the working precision; FP64 from the warp sums on
+    Real b_rain = 0, b_src = 0, b_ev = 0, b_out = 0, b_clamp = 0;
+    bool bad = false;
+    constexpr int OH = TH + 1, OW = TW + 1;  // rows/cols [3, TH+4) x [3, TW+4)
+    for (int k = tid; k < OH * OW; k += NT) {
+        const int r = 3 + k / OW, c = 3 + (k - (k / OW) * OW);
+        const int p = r * RW + c;
+        const int gi = I0 + r, gj = J0 + c;
+        const Real un = fix_x(p), us = fix_x(p + RW), vw = fix_y(p), ve = fix_y(p + 1);
+        Real hv = 0, hraw = 0;
+        const bool act = s_m[p] != 0;
+        Real ql = 0, rr = 0, pct = 0, evapo = 0;
+        if (act) {
+            const Real ho = s_h[p];
+            const bool hi = ho >= T.gt_evmin;
+            pct = hi ? pct_hi : pct_lo;
+            evapo = hi ? ev1 : Real(0.000);
+            for (int q = 0; q < nloc; q++)
+                if (s_srcp[q] == p) ql = s_srcq1[q];
+            rr = storm ? storm_rate(gi, gj, t1) : rr1_u;
+            hraw = ho - dt2 * ((us - un) / dx + (ve - vw) / dy - ql - rr * pct + evapo);
+            hv = fmax(hraw, Real(0.00));
+        }
+        s_h[p] = hv;  // the new depth; only this thread reads s_h[p] in this stage
+        s_umo[p] = un;
+        s_vno[p] = vw;
+        if (r == TH + 3) s_umo[p + RW] = us;
+        if (c == TW + 3) s_vno[p + 1] = ve;
+        const bool core = r >= HN && c >= HN && r < TH + HN && c < TW + HN && gi < rows && gj < cols;
+        if (core) {
+            const size_t gp = (size_t)gi * pitch + gj;
+            Hout[gp] = hv;
+            Uout[gp] = un;
+            Vout[gp] = vw;
+            if (gi == rows - 1) {
+                Uout[gp + pitch] = us;
+                b_out += us;
+            }
+            if (act) {
+                b_rain += rr * pct;
+                b_src += ql;
+                b_ev += evapo;
+                if (hraw < Real(0)) b_clamp -= hraw;
+            }
+            if (!RT<Real>::finite_(hv) || !RT<Real>::finite_(un) || !RT<Real>::finite_(vw)) bad = true;
+        }
+    }
+    __syncthreads();
+
+    // ---- stage 5: CFL bound of the new state over the owned faces ----------
+    Real cm = 0;
+    for (int k = tid; k < TH * TW; k += NT) {
+        const int r = HN + k / TW, c = HN + (k - (k / TW) * TW);
+        const int p = r * RW + c;
+        const int gi = I0 + r, gj = J0 + c;
+        if (gi >= rows || gj >= cols) continue;
+        if (gi > 0 && s_m[p] && s_m[p - RW]) {
+            const Real hm = Real(0.50) * (s_h[p] + s_h[p - RW]);
+            if (hm >= T.ge_th) {
+                const Real v = fabs(s_umo[p] / hm) + RT<Real>::sqrt_(g * hm);
+                cm = fmax(cm, v);
+            }
+        }
+        if (gi == rows - 1 && G.south_open && s_m[p]) {
+            const Real hm = s_h[p];
+            if (hm >= T.ge_th) {
+                const Real v = fabs(s_umo[p + RW] / hm) + RT<Real>::sqrt_(g * hm);
+                cm = fmax(cm, v);
+            }
+        }
+        if (gj > 0 && s_m[p] && s_m[p - 1]) {
+            const Real hn = Real(0.50) * (s_h[p] + s_h[p - 1]);
+            if (hn >= T.ge_th) {
+                const Real v = fabs(s_vno[p] / hn) + RT<Real>::sqrt_(g * hn);
+                cm = fmax(cm, v);
+            }
+        }
+    }
+
+    // ---- block reductions and one atomic per quantity ----------------------
+    double vals[B_N + 1] = {(double)b_rain, (double)b_src, (double)b_ev, (double)b_out, (double)b_clamp, (double)cm};
+    const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+    for (int q = 0; q < B_N; q++) {
+        double v = vals[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        vals[q] = v;
+    }
+    {
+        double v = vals[B_N];
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        vals[B_N] = v;
+    }
+    const bool any_bad = __syncthreads_or(bad);
+    if (lane == 0)
+        for (int q = 0; q <= B_N; q++) s_red[wid][q] = vals[q];
+    __syncthreads();
+    if (tid == 0) {
+        double acc[B_N + 1];
+        for (int q = 0; q <= B_N; q++) acc[q] = s_red[0][q];
+        for (int w = 1; w < NW; w++) {
+            for (int q = 0; q < B_N; q++) acc[q] += s_red[w][q];
+            acc[B_N] = fmax(acc[B_N], s_red[w][B_N]);
+        }
+        Clock &co = clk[slot_out];
+        const double area = G.dx * G.dy;
+        const double scale = dt2d * area;
+        if (acc[B_RAIN] != 0.0) atomicAdd(&co.step[B_RAIN], acc[B_RAIN] * scale);
+        if (acc[B_SRC] != 0.0) atomicAdd(&co.step[B_SRC], acc[B_SRC] * scale);
+        if (acc[B_EV] != 0.0) atomicAdd(&co.step[B_EV], acc[B_EV] * scale);
+        if (acc[B_OUT] != 0.0) atomicAdd(&co.step[B_OUT], acc[B_OUT] * dt2d * G.dy);
+        if (acc[B_CLAMP] != 0.0) atomicAdd(&co.step[B_CLAMP], acc[B_CLAMP] * area);
+        if (acc[B_N] > 0.0) atomicMax(&co.cmax_bits, (unsigned long long)__double_as_longlong(acc[B_N]));
+        if (any_bad) atomicOr(&co.nonfinite, 1u);
+    }
+}
+
+}  // namespace sw2d

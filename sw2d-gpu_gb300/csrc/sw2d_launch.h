@@ -1,0 +1,44 @@
+// sw2d_launch.h -- host launchers of the device kernels, one overload set per
+// working precision.  The FP64 set lives in step_f64.cu (compiled without
+// FMA contraction), the FP32 set in step_f32.cu (fast math).
+#pragma once
+
+#include "sw2d_device.cuh"
+
+namespace sw2d {
+
+// Core tiles supported by the step kernel instantiations.
+bool tile_supported(int precision, int th, int tw);
+void default_tile(int precision, int *th, int *tw);
+
+#define SW2D_DECLARE_LAUNCHERS(Real)                                                                          \
+    cudaError_t prepare_step(int th, int tw, Real tag);                                                      \
+    cudaError_t launch_step(int th, int tw, int nblocks, const GridDesc &G, const ForcingDesc &F,             \
+                            const StateBufs<Real> &S, const Thr<Real> &T, Clock *clk, const Control *ctl,    \
+                            int slot, cudaStream_t st);                                                      \
+    cudaError_t launch_pack_static(const double *z, const double *n, int rows, int cols, int pitch,         \
+                                   double nodata, Real *zout, Real *nout, uint8_t *mask, cudaStream_t st);   \
+    cudaError_t launch_pack_depth(const double *src, int rows, int cols, int pitch, const uint8_t *mask,     \
+                                  Real *dst, cudaStream_t st);                                               \
+    cudaError_t launch_pack_um(const double *src, int rows, int cols, int pitch, int south_open,             \
+                               const uint8_t *mask, Real *dst, cudaStream_t st);                             \
+    cudaError_t launch_pack_vn(const double *src, int rows, int cols, int pitch, const uint8_t *mask,        \
+                               Real *dst, cudaStream_t st);                                                  \
+    cudaError_t launch_unpack(const Real *src, int nr, int nc, int pitch, double *dst, cudaStream_t st);     \
+    cudaError_t launch_velocity(const Real *h, const Real *um, const Real *vn, int rows, int cols, int pitch, \
+                                Real ge_th, double *uu, double *vv, cudaStream_t st);                        \
+    cudaError_t launch_volume(const Real *h, const uint8_t *mask, int rows, int cols, int pitch,             \
+                              double *partial, int nblocks, cudaStream_t st);                                \
+    cudaError_t launch_cmax(const Real *h, const Real *um, const Real *vn, const uint8_t *mask, int rows,    \
+                            int cols, int pitch, int south_open, Real ge_th, double g,                       \
+                            unsigned long long *out, cudaStream_t st);                                       \
+    cudaError_t launch_probe(const Real *h, int rows, int cols, int pitch, const int *cells, int n,          \
+                             double *out, cudaStream_t st);
+
+SW2D_DECLARE_LAUNCHERS(double)
+SW2D_DECLARE_LAUNCHERS(float)
+
+constexpr int kVolumeBlocks = 1024;
+constexpr int kVolumeThreads = 256;
+
+}  // namespace sw2d

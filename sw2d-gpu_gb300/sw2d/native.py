@@ -1,0 +1,243 @@
+"""ctypes binding of the C ABI (include/sw2d.h) exported by libsw2d.so.
+
+This is the Python face of the drop-in boundary: every call goes straight to
+the native library; there is no Python or CPU fallback.  If the library is
+missing, loading fails with an error.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_ROOT, "_build", "libsw2d.so")
+HEADER = os.path.join(os.path.dirname(PKG_ROOT), "include", "sw2d.h")
+
+OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT, ERR_STATE = range(7)
+PREC_F64, PREC_F32 = 0, 1
+DT_FIXED, DT_CFL = 0, 1
+FIELD_DEPTH, FIELD_UM, FIELD_VN, FIELD_UU, FIELD_VV, FIELD_ELEVATION = range(6)
+RAIN_NONE, RAIN_COMPAT, RAIN_STEP, RAIN_LINEAR, RAIN_STORM = range(5)
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("rows", C.c_int32), ("cols", C.c_int32),
+        ("dx", C.c_double), ("dy", C.c_double), ("nodata", C.c_double),
+        ("g", C.c_double), ("th", C.c_double), ("manning", C.c_double),
+        ("INT", C.c_double), ("INF", C.c_double), ("LWL", C.c_double), ("EV_WL_min", C.c_double),
+        ("precision", C.c_int32), ("dt_mode", C.c_int32),
+        ("dt", C.c_double), ("cfl", C.c_double),
+        ("south_open", C.c_int32), ("device", C.c_int32),
+        ("tile_h", C.c_int32), ("tile_w", C.c_int32),
+        ("reserved", C.c_int32 * 4),
+    ]
+
+
+class Budget(C.Structure):
+    _fields_ = [
+        ("t", C.c_double), ("dt", C.c_double), ("cmax", C.c_double),
+        ("volume", C.c_double), ("volume0", C.c_double),
+        ("rain_in", C.c_double), ("source_in", C.c_double), ("evap_out", C.c_double),
+        ("outflow", C.c_double), ("clamp_gain", C.c_double),
+        ("steps", C.c_int64), ("nonfinite", C.c_int32), ("reserved", C.c_int32),
+    ]
+
+
+class SW2DError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+_lib = None
+
+# every function the header declares, with its ctypes signature
+_SIGS = {
+    "sw2d_config_init": (C.c_int, [C.POINTER(Config)]),
+    "sw2d_device_bytes": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_int64)]),
+    "sw2d_create": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_void_p)]),
+    "sw2d_destroy": (C.c_int, [C.c_void_p]),
+    "sw2d_set_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sw2d_set_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
+    "sw2d_set_rain": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_double]),
+    "sw2d_set_storm": (C.c_int, [C.c_void_p] + [C.c_double] * 7),
+    "sw2d_set_evaporation": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_double]),
+    "sw2d_set_point_sources": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_double]),
+    "sw2d_advance": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.POINTER(C.c_int64)]),
+    "sw2d_get_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "sw2d_get_budget": (C.c_int, [C.c_void_p, C.POINTER(Budget)]),
+    "sw2d_probe": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "sw2d_synchronize": (C.c_int, [C.c_void_p]),
+    "sw2d_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "sw2d_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "sw2d_last_error": (C.c_char_p, [C.c_void_p]),
+    "sw2d_status_string": (C.c_char_p, [C.c_int32]),
+}
+
+
+def exported_names():
+    return list(_SIGS)
+
+
+def load(path: str | None = None):
+    """Loads libsw2d.so (fails loudly when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OSError(f"{p} not found: build it with sw2d-gpu_gb300/build_native.py (no CPU fallback exists)")
+    L = C.CDLL(p)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f64(a, shape=None):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None and a.shape != shape:
+        a = a.reshape(shape)
+    return a
+
+
+def default_config(**kw) -> Config:
+    c = Config()
+    load().sw2d_config_init(C.byref(c))
+    for k, v in kw.items():
+        if not hasattr(c, k):
+            raise AttributeError(f"sw2d_config has no field {k}")
+        setattr(c, k, v)
+    return c
+
+
+def device_bytes(cfg: Config) -> int:
+    b = C.c_int64()
+    st = load().sw2d_device_bytes(C.byref(cfg), C.byref(b))
+    if st != OK:
+        raise SW2DError(st, "sw2d_device_bytes")
+    return int(b.value)
+
+
+class Solver:
+    """One scenario on the GPU, owned through a C-ABI handle."""
+
+    def __init__(self, cfg: Config | None = None, **kw):
+        L = load()
+        self.cfg = cfg if cfg is not None else default_config(**kw)
+        h = C.c_void_p()
+        st = L.sw2d_create(C.byref(self.cfg), C.byref(h))
+        if st != OK:
+            raise SW2DError(st, "sw2d_create failed: " + L.sw2d_status_string(st).decode())
+        self._h = h
+        self.rows, self.cols = self.cfg.rows, self.cfg.cols
+
+    def _check(self, st, what):
+        if st != OK:
+            msg = load().sw2d_last_error(self._h).decode()
+            raise SW2DError(st, f"{what}: {msg}")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().sw2d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- inputs ---------------------------------------------------------
+    def set_static(self, z, manning=None):
+        r, c = self.rows, self.cols
+        z = _f64(z, (r, c))
+        n = _f64(manning, (r, c)) if manning is not None else None
+        self._check(load().sw2d_set_static(self._h, _p(z), _p(n)), "sw2d_set_static")
+
+    def set_state(self, depth, um=None, vn=None, t0=0.0):
+        r, c = self.rows, self.cols
+        d = _f64(depth, (r, c))
+        u = _f64(um, (r + 1, c)) if um is not None else None
+        v = _f64(vn, (r, c + 1)) if vn is not None else None
+        self._check(load().sw2d_set_state(self._h, _p(d), _p(u), _p(v), float(t0)), "sw2d_set_state")
+
+    def set_rain(self, kind, series=None, dt_series=1.0):
+        s = _f64(np.atleast_1d(series)) if series is not None else None
+        n = 0 if s is None else s.size
+        self._check(load().sw2d_set_rain(self._h, int(kind), _p(s), n, float(dt_series)), "sw2d_set_rain")
+
+    def set_storm(self, peak, x0, y0, vx, vy, sigma, t_stop=1e300):
+        self._check(load().sw2d_set_storm(self._h, peak, x0, y0, vx, vy, sigma, t_stop), "sw2d_set_storm")
+
+    def set_evaporation(self, series=None, dt_series=1.0):
+        s = _f64(np.atleast_1d(series)) if series is not None else None
+        n = 0 if s is None else s.size
+        self._check(load().sw2d_set_evaporation(self._h, _p(s), n, float(dt_series)), "sw2d_set_evaporation")
+
+    def set_point_sources(self, cells, q, dtoq):
+        cells = np.ascontiguousarray(cells, dtype=np.int32)
+        q = _f64(np.asarray(q).reshape(-1, max(cells.size, 1)))
+        self._check(load().sw2d_set_point_sources(self._h, _p(cells), cells.size, _p(q), q.shape[0], float(dtoq)),
+                    "sw2d_set_point_sources")
+
+    # -- running --------------------------------------------------------
+    def advance(self, max_steps, t_end=1e300):
+        done = C.c_int64()
+        self._check(load().sw2d_advance(self._h, int(max_steps), float(t_end), C.byref(done)), "sw2d_advance")
+        return int(done.value)
+
+    def synchronize(self):
+        self._check(load().sw2d_synchronize(self._h), "sw2d_synchronize")
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._check(load().sw2d_get_stream(self._h, C.byref(s)), "sw2d_get_stream")
+        return int(s.value or 0)
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        self._check(load().sw2d_launch_count(self._h, C.byref(n)), "sw2d_launch_count")
+        return int(n.value)
+
+    # -- outputs --------------------------------------------------------
+    def field(self, which):
+        r, c = self.rows, self.cols
+        shape = {FIELD_UM: (r + 1, c), FIELD_VN: (r, c + 1)}.get(which, (r, c))
+        out = np.empty(shape, dtype=np.float64)
+        self._check(load().sw2d_get_field(self._h, int(which), _p(out)), "sw2d_get_field")
+        return out
+
+    def depth(self):
+        return self.field(FIELD_DEPTH)
+
+    def state(self):
+        return {"h": self.field(FIELD_DEPTH), "um": self.field(FIELD_UM), "vn": self.field(FIELD_VN)}
+
+    def budget(self):
+        b = Budget()
+        self._check(load().sw2d_get_budget(self._h, C.byref(b)), "sw2d_get_budget")
+        return {k: getattr(b, k) for k, _ in Budget._fields_ if k != "reserved"}
+
+    def probe(self, cells):
+        cells = np.ascontiguousarray(cells, dtype=np.int32)
+        out = np.empty(cells.size, dtype=np.float64)
+        self._check(load().sw2d_probe(self._h, _p(cells), cells.size, _p(out)), "sw2d_probe")
+        return out

@@ -1,0 +1,59 @@
+"""Size-independent properties of the oracle (CPU): conservation, symmetry,
+determinism across thread counts, the CFL rule, walls."""
+import numpy as np
+import pytest
+
+
+def _dam(O, rows=32, cols=64, **kw):
+    from sw2d import scenarios as S
+    s = S.dam_break_channel(rows, cols, 1.0, x_gate=cols / 2)
+    o = O.Oracle(rows, cols, 1.0, 1.0, s["z"], manning=kw.pop("manning", 0.0), dt_mode=1, dt=1.0, cfl=0.5, **kw)
+    o.set_state(s["h0"])
+    return o, s
+
+
+def test_volume_conserved_with_walls(oracle_mod):
+    o, s = _dam(oracle_mod)
+    v0 = o.volume()
+    o.advance(300)
+    b = o.budget()
+    assert abs(o.volume() + 0.0 - v0 - b["clamp_gain"]) / v0 < 1e-12
+
+
+def test_row_symmetry(oracle_mod):
+    """A 1D dam break stays identical across rows (walls north and south)."""
+    o, s = _dam(oracle_mod)
+    o.advance(200)
+    h = o.state()["h"]
+    assert np.array_equal(h, np.repeat(h[:1], h.shape[0], axis=0))
+
+
+def test_thread_count_does_not_change_results(oracle_mod):
+    o1, _ = _dam(oracle_mod, threads=1)
+    o1.advance(50)
+    h1 = o1.state()["h"]
+    o2, _ = _dam(oracle_mod, threads=4)
+    o2.advance(50)
+    assert np.array_equal(h1, o2.state()["h"])
+    oracle_mod.lib().orc_set_threads(oracle_mod.max_threads())
+
+
+def test_cfl_rule_initial_step(oracle_mod):
+    o, _ = _dam(oracle_mod)
+    # dt2 = 0.5 * dx / sqrt(g h) with h = 10 at the still, wet faces
+    assert o.next_dt() * 2 == pytest.approx(0.5 / np.sqrt(9.8 * 10.0), rel=1e-15)
+
+
+def test_fixed_dt_time_accumulates_like_reference(oracle_mod):
+    from sw2d import scenarios as S
+    s = S.dam_break_channel(8, 16, 1.0, x_gate=8)
+    o = oracle_mod.Oracle(8, 16, 1.0, 1.0, s["z"], dt_mode=0, dt=0.04)
+    o.set_state(s["h0"])
+    n = o.advance(10 ** 9, t_end=1.0)
+    t = 0.0
+    k = 0
+    while t + 0.04 <= 1.0:  # cu:1256, time += dt twice (cu:1297, cu:1335)
+        t = t + 0.04
+        t = t + 0.04
+        k += 1
+    assert n == k and o.state()["t"] == t
