@@ -109,6 +109,86 @@ static void kadd(kahan *k, double v) {
     k->s = t;
 }
 
+/* ---- deterministic log / exp / power ------------------------------------
+ * The friction term raises the face depth to 1.3333330 (cu:195, cu:312) and
+ * the storm forcing needs exp().  Library pow/exp differ by ulps between
+ * glibc and CUDA, and near the wet/dry threshold such ulps grow into
+ * visible depth differences.  The oracle and the FP64 device path therefore
+ * both use this routine, built only from IEEE-exact + - * / (no FMA), so the
+ * two give identical bits:
+ *   log: x = m 2^e, m in [1/sqrt2, sqrt2), log m = 2 atanh(s) with
+ *        s = (m-1)/(m+1) (|s| <= 0.1716) summed to s^21/21 (Horner);
+ *   exp: Cody-Waite reduction y = k ln2 + r, |r| <= ln2/2, Taylor series
+ *        of e^r to r^13/13!, scaled by 2^k built from its bit pattern;
+ *   ln2 split into a 21-bit head (exact k*LN2_HI) and a tail.
+ * Both are accurate to a few ulps (checked against glibc pow in tests). */
+#define ORC_LN2_HI 0x1.62e42p-1
+#define ORC_LN2_LO 0x1.fdf473de6af28p-22
+#define ORC_INV_LN2 0x1.71547652b82fep+0
+
+static double bits2d(uint64_t b) { double d; memcpy(&d, &b, 8); return d; }
+static uint64_t d2bits(double d) { uint64_t b; memcpy(&b, &d, 8); return b; }
+
+double orc_log(double x) {
+    uint64_t b = d2bits(x);
+    int e = (int)((b >> 52) & 0x7ff) - 1023;
+    double m = bits2d((b & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL);
+    if (m > 1.4142135623730951) {
+        m = m * 0.5;
+        e += 1;
+    }
+    double s = (m - 1.0) / (m + 1.0);
+    double s2 = s * s;
+    double p = 1.0 / 21.0;
+    p = p * s2 + 1.0 / 19.0;
+    p = p * s2 + 1.0 / 17.0;
+    p = p * s2 + 1.0 / 15.0;
+    p = p * s2 + 1.0 / 13.0;
+    p = p * s2 + 1.0 / 11.0;
+    p = p * s2 + 1.0 / 9.0;
+    p = p * s2 + 1.0 / 7.0;
+    p = p * s2 + 1.0 / 5.0;
+    p = p * s2 + 1.0 / 3.0;
+    p = p * s2 + 1.0;
+    double lm = 2.0 * s * p;
+    double ef = (double)e;
+    return ef * ORC_LN2_HI + (ef * ORC_LN2_LO + lm);
+}
+
+double orc_exp(double y) {
+    if (y < -700.0) return 0.0;
+    if (y > 700.0) return HUGE_VAL;
+    double kf = floor(y * ORC_INV_LN2 + 0.5);
+    double r = (y - kf * ORC_LN2_HI) - kf * ORC_LN2_LO;
+    double p = 1.0 / 6227020800.0;
+    p = p * r + 1.0 / 479001600.0;
+    p = p * r + 1.0 / 39916800.0;
+    p = p * r + 1.0 / 3628800.0;
+    p = p * r + 1.0 / 362880.0;
+    p = p * r + 1.0 / 40320.0;
+    p = p * r + 1.0 / 5040.0;
+    p = p * r + 1.0 / 720.0;
+    p = p * r + 1.0 / 120.0;
+    p = p * r + 1.0 / 24.0;
+    p = p * r + 1.0 / 6.0;
+    p = p * r + 0.5;
+    p = p * r + 1.0;
+    p = p * r + 1.0;
+    int k = (int)kf;
+    return p * bits2d((uint64_t)(k + 1023) << 52);
+}
+
+/* hm^1.3333330 of the friction term (cu:195, cu:312), for hm > th > 0 */
+double orc_pow43(double x) { return orc_exp(1.3333330 * orc_log(x)); }
+
+void orc_pow43_vec(const double *x, int n, double *out) {
+    for (int k = 0; k < n; k++) out[k] = orc_pow43(x[k]);
+}
+
+void orc_exp_vec(const double *x, int n, double *out) {
+    for (int k = 0; k < n; k++) out[k] = orc_exp(x[k]);
+}
+
 /* ---- host forcing, restating cu:526-555 and cu:589-601 ---------------- */
 
 /* The reference's interpolation divides by the elapsed time inside the
@@ -156,7 +236,7 @@ static double rain_cell(const orc_forcing *f, const orc_params *p, double t, int
     double x = ((double)j + 0.5) * p->dx - xc;
     double y = ((double)i + 0.5) * p->dy - yc;
     double s2 = f->storm_sigma * f->storm_sigma;
-    return f->storm_peak / 3.6e6 * exp(-(x * x + y * y) / (2.0 * s2));
+    return f->storm_peak / 3.6e6 * orc_exp(-(x * x + y * y) / (2.0 * s2));
 }
 
 static double evap_rate(const orc_forcing *f, double t) {
@@ -359,7 +439,7 @@ static void momentum(const orc_params *p, const double *h, const double *z, cons
                             ram = 0.00;
                         } else {
                             double sqx = sqrt(w->uu1[e] * w->uu1[e] + w->vva[e] * w->vva[e]);
-                            double expx = pow(hmv, 1.3333330);
+                            double expx = orc_pow43(hmv);
                             ram = g * rn * rn * sqx / expx;
                         }
                         /* cu:203 */
@@ -416,7 +496,7 @@ static void momentum(const orc_params *p, const double *h, const double *z, cons
                             ram = 0.00;
                         } else {
                             double sqy = sqrt(w->uua[YI(i, j)] * w->uua[YI(i, j)] + vv_c * vv_c);
-                            double expy = pow(hnv, 1.3333330);
+                            double expy = orc_pow43(hnv);
                             ram = g * rn * rn * sqy / expy;
                         }
                         out = ((1.00 - dt2 * ram * 0.50) * mo_c + (-v11 - v12 - v13)) / (1.00 + dt2 * ram * 0.50); /* cu:320 */

@@ -180,6 +180,17 @@ int capture_graph(sw2d_handle *h) {
     return SW2D_OK;
 }
 
+void sync_grid_scalars(GridDesc &G) {
+    G.sf.dx = (float)G.sd.dx;
+    G.sf.dy = (float)G.sd.dy;
+    G.sf.g = (float)G.sd.g;
+    G.sf.manning = (float)G.sd.manning;
+    G.sf.pct_hi = (float)G.sd.pct_hi;
+    G.sf.pct_lo = (float)G.sd.pct_lo;
+    G.sf.storm_amp = (float)G.sd.storm_amp;
+    G.sf.storm_2s2 = (float)G.sd.storm_2s2;
+}
+
 template <class T>
 int upload_table(sw2d_handle *h, DevBuf &b, const T *src, size_t n) {
     const size_t bytes = n * sizeof(T);
@@ -205,9 +216,8 @@ bool tile_supported(int precision, int th, int tw) {
 }
 
 void default_tile(int precision, int *th, int *tw) {
-    *th = 16;
+    *th = precision == SW2D_PREC_F64 ? 16 : 32;
     *tw = 32;
-    (void)precision;
 }
 
 }  // namespace sw2d
@@ -303,9 +313,15 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
     G.cfl = cfg->cfl;
     G.dmin = cfg->dx < cfg->dy ? cfg->dx : cfg->dy;
     G.dt_half = cfg->dt;
-    G.pct_hi = 1.00 - cfg->LWL;               // cu:628
-    G.pct_lo = 1.00 - (cfg->INT + cfg->INF);  // cu:632
-    G.manning = cfg->manning;
+    G.sd.dx = cfg->dx;
+    G.sd.dy = cfg->dy;
+    G.sd.g = cfg->g;
+    G.sd.manning = cfg->manning;
+    G.sd.pct_hi = 1.00 - cfg->LWL;               // cu:628
+    G.sd.pct_lo = 1.00 - (cfg->INT + cfg->INF);  // cu:632
+    G.sd.storm_amp = 0.0;
+    G.sd.storm_2s2 = 1.0;
+    sync_grid_scalars(G);
     h->F.rain_kind = RAIN_NONE;
     h->F.rain_dt = 1.0;
     h->F.ev_dt = 1.0;
@@ -448,6 +464,9 @@ int sw2d_set_storm(sw2d_handle *h, double peak, double x0, double y0, double vx,
     h->F.storm_vy = vy;
     h->F.storm_sigma = sigma;
     h->F.storm_tstop = t_stop;
+    h->G.sd.storm_amp = peak / 3.6e6;                // mm/h -> m/s
+    h->G.sd.storm_2s2 = 2.0 * (sigma * sigma);
+    sync_grid_scalars(h->G);
     h->graph_valid = false;
     return SW2D_OK;
 }
@@ -507,6 +526,9 @@ int sw2d_advance(sw2d_handle *h, int64_t max_steps, double t_end, int64_t *steps
     ctl.step_limit = start + max_steps;
     *h->h_ctl = ctl;
     CK(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Control), cudaMemcpyHostToDevice, h->stream));
+    // plan the next launch under the new control and the current forcing
+    plan_kernel<<<1, 1, 0, h->stream>>>(h->G, h->F, h->d_clk, h->d_ctl, (int)(h->launches % 3));
+    CK(h, cudaGetLastError());
     for (;;) {
         double dtn;
         double cmax;

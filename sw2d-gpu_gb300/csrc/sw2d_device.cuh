@@ -46,10 +46,28 @@ enum { ST_TOO_MANY_LOCAL_SOURCES = 1 };
 
 constexpr int kMaxLocalSources = 64;
 
+// What one launch does, computed once per launch (never per thread: FP64
+// arithmetic runs at a small fraction of the FP32 rate on this GPU).
+template <class Real>
+struct LaunchScalars {
+    Real dt2;                  // 2 dt (cu:808)
+    Real dt2dx, dt2dy;         // dt2/dx, dt2/dy as in cu:166, cu:283
+    Real rr0, rr1, ev0, ev1;   // uniform rain / evaporation at t0 and t1 [m/s]
+    Real sx0, sy0, sx1, sy1;   // storm centre at t0 and t1 [m]
+};
+
+struct Plan {
+    int run, storm_on0, storm_on1, pad;
+    double t0, t1, dt;         // t1 = t0 + dt (cu:1297)
+    LaunchScalars<double> d;   // FP64 values
+    LaunchScalars<float> f;    // the same, rounded once to FP32
+};
+
 // Per-iteration bookkeeping.  Three slots rotate: launch m reads slot m%3,
-// writes slot (m+1)%3 and clears the accumulators of slot (m+2)%3, which is
-// the one launch m+1 will write.  So no launch ever reads a slot that a
-// concurrent CTA is still accumulating into.
+// accumulates into slot (m+1)%3, and its last CTA to finish finalises that
+// slot (time, plan of launch m+1) and clears slot (m+2)%3 for launch m+1.
+// No launch reads a slot that its own CTAs are still accumulating into, and
+// no CTA ever waits for another.
 struct __align__(16) Clock {
     double t;                      // time at the start of the next iteration
     double dt;                     // half step of the last iteration
@@ -61,6 +79,9 @@ struct __align__(16) Clock {
     unsigned int status;           // device-side error bits (sticky)
     double tot_s[B_N], tot_c[B_N]; // Kahan running totals of the budgets [m^3]
     double step[B_N];              // budget sums of the iteration that wrote this slot
+    unsigned int done_blocks;      // CTAs of the writing launch that have finished
+    unsigned int pad;
+    Plan plan;                     // what the launch reading this slot does
 };
 
 struct Control {
@@ -68,13 +89,33 @@ struct Control {
     long long step_limit;
 };
 
+template <class Real>
+struct GridScalars {
+    Real dx, dy, g, manning;
+    Real pct_hi, pct_lo;       // 1 - LWL and 1 - (INT + INF)   (cu:627-634)
+    Real storm_amp, storm_2s2; // peak/3.6e6 [m/s] and 2 sigma^2 [m^2]
+};
+
 struct GridDesc {
     int rows, cols, pitch, tiles_w;
     int dt_mode, south_open, n_src, pad0;
     double dx, dy, g, th, cfl, dmin, dt_half;
-    double pct_hi, pct_lo;  // 1 - LWL and 1 - (INT + INF)   (cu:627-634)
-    double manning;
+    GridScalars<double> sd;    // FP64 values
+    GridScalars<float> sf;     // the same, rounded once to FP32
 };
+
+template <class Real>
+__device__ __forceinline__ const LaunchScalars<Real> &launch_scalars(const Plan &p);
+template <>
+__device__ __forceinline__ const LaunchScalars<double> &launch_scalars<double>(const Plan &p) { return p.d; }
+template <>
+__device__ __forceinline__ const LaunchScalars<float> &launch_scalars<float>(const Plan &p) { return p.f; }
+template <class Real>
+__device__ __forceinline__ const GridScalars<Real> &grid_scalars(const GridDesc &g);
+template <>
+__device__ __forceinline__ const GridScalars<double> &grid_scalars<double>(const GridDesc &g) { return g.sd; }
+template <>
+__device__ __forceinline__ const GridScalars<float> &grid_scalars<float>(const GridDesc &g) { return g.sf; }
 
 struct ForcingDesc {
     int rain_kind, n_rain, n_ev, n_qrec;
@@ -187,6 +228,113 @@ __device__ inline double source_rate(const ForcingDesc &F, int n_src, int s, dou
     return q / area;
 }
 
+// The plan of the launch that reads clock slot c under control ctl.
+__device__ inline Plan make_plan(double t, unsigned long long cmax_bits, long long steps, const Control &ctl,
+                                 const GridDesc &G, const ForcingDesc &F) {
+    Plan p;
+    p.run = 0;
+    p.storm_on0 = p.storm_on1 = 0;
+    p.pad = 0;
+    p.t0 = t;
+    p.t1 = t;
+    p.dt = 0.0;
+    LaunchScalars<double> &d = p.d;
+    d.dt2 = d.dt2dx = d.dt2dy = 0.0;
+    d.rr0 = d.rr1 = d.ev0 = d.ev1 = 0.0;
+    d.sx0 = d.sy0 = d.sx1 = d.sy1 = 0.0;
+    double dt = 0.0;
+    if (decide_step(t, __longlong_as_double((long long)cmax_bits), steps, ctl, G, &dt)) {
+        p.run = 1;
+        p.dt = dt;
+        p.t1 = t + dt;
+        d.dt2 = 2.00 * dt;
+        d.dt2dx = d.dt2 / G.dx;
+        d.dt2dy = d.dt2 / G.dy;
+        d.rr0 = rain_uniform(F, p.t0);
+        d.rr1 = rain_uniform(F, p.t1);
+        d.ev0 = evap_rate(F, p.t0);
+        d.ev1 = evap_rate(F, p.t1);
+        if (F.rain_kind == RAIN_STORM) {
+            p.storm_on0 = p.t0 < F.storm_tstop;
+            p.storm_on1 = p.t1 < F.storm_tstop;
+            d.sx0 = F.storm_x0 + F.storm_vx * p.t0;
+            d.sy0 = F.storm_y0 + F.storm_vy * p.t0;
+            d.sx1 = F.storm_x0 + F.storm_vx * p.t1;
+            d.sy1 = F.storm_y0 + F.storm_vy * p.t1;
+        }
+    }
+    LaunchScalars<float> &f = p.f;
+    f.dt2 = (float)d.dt2;
+    f.dt2dx = (float)d.dt2dx;
+    f.dt2dy = (float)d.dt2dy;
+    f.rr0 = (float)d.rr0;
+    f.rr1 = (float)d.rr1;
+    f.ev0 = (float)d.ev0;
+    f.ev1 = (float)d.ev1;
+    f.sx0 = (float)d.sx0;
+    f.sy0 = (float)d.sy0;
+    f.sx1 = (float)d.sx1;
+    f.sy1 = (float)d.sy1;
+    return p;
+}
+
+// ---------------------------------------------------------------------------
+// deterministic FP64 log / exp / power.  Same algorithm and operation order
+// as the oracle's (log: atanh series on m in [1/sqrt2, sqrt2); exp:
+// Cody-Waite reduction by ln2 split into a 21-bit head and a tail, Taylor
+// series to r^13/13!, scaling by 2^k from its bit pattern), compiled without
+// FMA contraction, so the FP64 path and the oracle agree to the bit where
+// the reference uses pow (cu:195, cu:312).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double det_log(double x) {
+    const long long b = __double_as_longlong(x);
+    int e = (int)((b >> 52) & 0x7ff) - 1023;
+    double m = __longlong_as_double((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+    if (m > 1.4142135623730951) {
+        m = m * 0.5;
+        e += 1;
+    }
+    const double s = (m - 1.0) / (m + 1.0);
+    const double s2 = s * s;
+    double p = 1.0 / 21.0;
+    p = p * s2 + 1.0 / 19.0;
+    p = p * s2 + 1.0 / 17.0;
+    p = p * s2 + 1.0 / 15.0;
+    p = p * s2 + 1.0 / 13.0;
+    p = p * s2 + 1.0 / 11.0;
+    p = p * s2 + 1.0 / 9.0;
+    p = p * s2 + 1.0 / 7.0;
+    p = p * s2 + 1.0 / 5.0;
+    p = p * s2 + 1.0 / 3.0;
+    p = p * s2 + 1.0;
+    const double lm = 2.0 * s * p;
+    const double ef = (double)e;
+    return ef * 0x1.62e42p-1 + (ef * 0x1.fdf473de6af28p-22 + lm);
+}
+
+__device__ __forceinline__ double det_exp(double y) {
+    if (y < -700.0) return 0.0;
+    if (y > 700.0) return __longlong_as_double(0x7ff0000000000000LL);
+    const double kf = floor(y * 0x1.71547652b82fep+0 + 0.5);
+    const double r = (y - kf * 0x1.62e42p-1) - kf * 0x1.fdf473de6af28p-22;
+    double p = 1.0 / 6227020800.0;
+    p = p * r + 1.0 / 479001600.0;
+    p = p * r + 1.0 / 39916800.0;
+    p = p * r + 1.0 / 3628800.0;
+    p = p * r + 1.0 / 362880.0;
+    p = p * r + 1.0 / 40320.0;
+    p = p * r + 1.0 / 5040.0;
+    p = p * r + 1.0 / 720.0;
+    p = p * r + 1.0 / 120.0;
+    p = p * r + 1.0 / 24.0;
+    p = p * r + 1.0 / 6.0;
+    p = p * r + 0.5;
+    p = p * r + 1.0;
+    p = p * r + 1.0;
+    const int k = (int)kf;
+    return p * __longlong_as_double((long long)(k + 1023) << 52);
+}
+
 // ---------------------------------------------------------------------------
 // precision traits
 // ---------------------------------------------------------------------------
@@ -196,8 +344,8 @@ struct RT;
 template <>
 struct RT<double> {
     static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
-    static __device__ __forceinline__ double pow_(double x) { return pow(x, 1.3333330); }  // cu:195
-    static __device__ __forceinline__ double exp_(double x) { return exp(x); }
+    static __device__ __forceinline__ double pow_(double x) { return det_exp(1.3333330 * det_log(x)); }  // cu:195
+    static __device__ __forceinline__ double exp_(double x) { return det_exp(x); }
     static __device__ __forceinline__ bool finite_(double x) { return isfinite(x); }
 };
 
@@ -281,45 +429,46 @@ __global__ void __launch_bounds__(NT)
     Real *s_n = s_hs + RN;     // Manning n per cell (only if G has a raster)
     uint8_t *s_m = reinterpret_cast<uint8_t *>(s_n + RN);
 
-    __shared__ double s_red[NW][B_N + 1];
+    __shared__ Real s_red[NW][B_N + 1];
     __shared__ int s_nloc;
     __shared__ int s_srcp[kMaxLocalSources];
     __shared__ Real s_srcq0[kMaxLocalSources], s_srcq1[kMaxLocalSources];
     __shared__ int s_wcnt[NW];
-    __shared__ double s_f[4];  // rain(t), rain(t+dt), evap(t), evap(t+dt)
 
     const int tid = threadIdx.x;
     const int slot_out = slot == 2 ? 0 : slot + 1;
     const int slot_nx = slot == 0 ? 2 : slot - 1;
     const Clock &ci = clk[slot];
-    const double t0 = ci.t;
-    double dt = 0.0;
-    const bool run = decide_step(t0, __longlong_as_double((long long)ci.cmax_bits), ci.steps, *ctl, G, &dt);
+    const Plan pl = ci.plan;
 
-    if (blockIdx.x == 0 && tid == 0) {
-        Clock &co = clk[slot_out];
-        for (int k = 0; k < B_N; k++) {  // fold the previous iteration's sums (Kahan)
-            double s = ci.tot_s[k], c = ci.tot_c[k];
-            double y = ci.step[k] - c;
-            double tt = s + y;
-            co.tot_c[k] = (tt - s) - y;
-            co.tot_s[k] = tt;
+    if (!pl.run) {  // nothing to do: carry the state's clock forward
+        if (blockIdx.x == 0 && tid == 0) {
+            Clock &co = clk[slot_out];
+            for (int k = 0; k < B_N; k++) {
+                double s = ci.tot_s[k], c = ci.tot_c[k];
+                double y = ci.step[k] - c;
+                double tt = s + y;
+                co.tot_c[k] = (tt - s) - y;
+                co.tot_s[k] = tt;
+            }
+            co.t = ci.t;
+            co.dt = ci.dt;
+            co.steps = ci.steps;
+            co.buf = ci.buf;
+            co.ran = 0;
+            co.cmax_bits = ci.cmax_bits;
+            co.nonfinite = ci.nonfinite;
+            co.status = ci.status;
+            co.plan = pl;
+            Clock &cn = clk[slot_nx];
+            cn.cmax_bits = 0ull;
+            cn.nonfinite = 0u;
+            cn.status = 0u;
+            cn.done_blocks = 0u;
+            for (int k = 0; k < B_N; k++) cn.step[k] = 0.0;
         }
-        co.t = run ? (t0 + dt) + dt : t0;  // cu:1297, cu:1335
-        co.dt = run ? dt : ci.dt;
-        co.steps = ci.steps + (run ? 1 : 0);
-        co.buf = run ? 1 - ci.buf : ci.buf;
-        co.ran = run ? 1 : 0;
-        if (!run) co.cmax_bits = ci.cmax_bits;
-        atomicOr(&co.nonfinite, ci.nonfinite);
-        atomicOr(&co.status, ci.status);
-        Clock &cn = clk[slot_nx];
-        cn.cmax_bits = 0ull;
-        cn.nonfinite = 0u;
-        cn.status = 0u;
-        for (int k = 0; k < B_N; k++) cn.step[k] = 0.0;
+        return;
     }
-    if (!run) return;
 
     const int rows = G.rows, cols = G.cols, pitch = G.pitch;
     const int ti = blockIdx.x / G.tiles_w, tj = blockIdx.x - ti * G.tiles_w;
@@ -333,12 +482,12 @@ __global__ void __launch_bounds__(NT)
     Real *__restrict__ Vout = S.vn[1 - buf];
     const bool has_n = S.nman != nullptr;
 
-    const double t1 = t0 + dt;  // time of the second continuity call (cu:1297)
-    const double dt2d = 2.00 * dt;  // cu:808
-    const Real dt2 = (Real)dt2d;
-    const Real dx = (Real)G.dx, dy = (Real)G.dy, g = (Real)G.g;
-    const Real dt2dx = (Real)(dt2d / G.dx), dt2dy = (Real)(dt2d / G.dy);
-    const Real manning = (Real)G.manning;
+    const LaunchScalars<Real> LS = launch_scalars<Real>(pl);
+    const GridScalars<Real> &GS = grid_scalars<Real>(G);
+    const Real dt2 = LS.dt2;
+    const Real dx = GS.dx, dy = GS.dy, g = GS.g;
+    const Real dt2dx = LS.dt2dx, dt2dy = LS.dt2dy;
+    const Real manning = GS.manning;
 
     // ---- stage 0: stage the tile + halo in shared memory --------------------
     for (int idx = tid; idx < RN; idx += NT) {
@@ -361,13 +510,7 @@ __global__ void __launch_bounds__(NT)
         s_umo[idx] = ((unsigned)gi <= (unsigned)rows && in_c) ? Uin[gp] : Real(0);
         s_vno[idx] = (in_r && (unsigned)gj <= (unsigned)cols) ? Vin[gp] : Real(0);
     }
-    if (tid == 0) {
-        s_f[0] = rain_uniform(F, t0);
-        s_f[1] = rain_uniform(F, t1);
-        s_f[2] = evap_rate(F, t0);
-        s_f[3] = evap_rate(F, t1);
-        s_nloc = 0;
-    }
+    if (tid == 0) s_nloc = 0;
     // point sources inside this tile's provisional-depth region, kept in
     // list order so that a later source on the same cell wins (cu:545)
     if (G.n_src > 0) {
@@ -394,8 +537,8 @@ __global__ void __launch_bounds__(NT)
                 off += __popc(bal & ((1u << lane) - 1u));
                 if (off < kMaxLocalSources) {
                     s_srcp[off] = p;
-                    s_srcq0[off] = (Real)source_rate(F, G.n_src, s, t0, area);
-                    s_srcq1[off] = (Real)source_rate(F, G.n_src, s, t1, area);
+                    s_srcq0[off] = (Real)source_rate(F, G.n_src, s, pl.t0, area);
+                    s_srcq1[off] = (Real)source_rate(F, G.n_src, s, pl.t1, area);
                 } else {
                     atomicOr(&clk[slot_out].status, (unsigned)ST_TOO_MANY_LOCAL_SOURCES);
                 }
@@ -411,10 +554,10 @@ __global__ void __launch_bounds__(NT)
     }
     __syncthreads();
 
-    const Real rr0_u = (Real)s_f[0], rr1_u = (Real)s_f[1];
-    const Real ev0 = (Real)s_f[2], ev1 = (Real)s_f[3];
+    const Real rr0_u = LS.rr0, rr1_u = LS.rr1;
+    const Real ev0 = LS.ev0, ev1 = LS.ev1;
     const int nloc = s_nloc;
-    const Real pct_hi = (Real)G.pct_hi, pct_lo = (Real)G.pct_lo;
+    const Real pct_hi = GS.pct_hi, pct_lo = GS.pct_lo;
     const bool storm = F.rain_kind == RAIN_STORM;
 
     // ---- stage 1: face depths and velocities (cu:363-453) ------------------
@@ -533,16 +676,15 @@ __global__ void __launch_bounds__(NT)
     }
     __syncthreads();
 
-    // storm rain at a cell centre
-    auto storm_rate = [&](int gi, int gj, double tt) -> Real {
-        if (tt >= F.storm_tstop) return Real(0);
-        const Real xc = (Real)(F.storm_x0 + F.storm_vx * tt);
-        const Real yc = (Real)(F.storm_y0 + F.storm_vy * tt);
-        const Real x = ((Real)gj + Real(0.5)) * dx - xc;
-        const Real y = ((Real)gi + Real(0.5)) * dy - yc;
-        const Real s2 = (Real)F.storm_sigma * (Real)F.storm_sigma;
-        return (Real)(F.storm_peak / 3.6e6) * RT<Real>::exp_(-(x * x + y * y) / (Real(2.0) * s2));
+    // storm rain at a cell centre; the centre (sx, sy) is per launch
+    const Real storm_amp = GS.storm_amp, storm_2s2 = GS.storm_2s2;
+    auto storm_rate = [&](int gi, int gj, bool on, Real sx, Real sy) -> Real {
+        if (!on) return Real(0);
+        const Real x = ((Real)gj + Real(0.5)) * dx - sx;
+        const Real y = ((Real)gi + Real(0.5)) * dy - sy;
+        return storm_amp * RT<Real>::exp_(-(x * x + y * y) / storm_2s2);
     };
+    const Real sx0 = LS.sx0, sy0 = LS.sy0, sx1 = LS.sx1, sy1 = LS.sy1;
 
     // ---- stage 3: provisional depth with forcing at t (cu:1278-1288) -------
     constexpr int PH = TH + 3, PW = TW + 3;  // rows/cols [2, TH+5) x [2, TW+5)
@@ -558,7 +700,7 @@ __global__ void __launch_bounds__(NT)
             Real ql = 0;
             for (int q = 0; q < nloc; q++)
                 if (s_srcp[q] == p) ql = s_srcq0[q];
-            const Real rr = storm ? storm_rate(I0 + r, J0 + c, t0) : rr0_u;
+            const Real rr = storm ? storm_rate(I0 + r, J0 + c, pl.storm_on0, sx0, sy0) : rr0_u;
             hv = ho - dt2 * ((s_rum[p + RW] - s_rum[p]) / dx + (s_rvn[p + 1] - s_rvn[p]) / dy - ql - rr * pct + evapo);
             hv = fmax(hv, Real(0.00));  // cu:657
         }
@@ -600,7 +742,7 @@ __global__ void __launch_bounds__(NT)
             evapo = hi ? ev1 : Real(0.000);
             for (int q = 0; q < nloc; q++)
                 if (s_srcp[q] == p) ql = s_srcq1[q];
-            rr = storm ? storm_rate(gi, gj, t1) : rr1_u;
+            rr = storm ? storm_rate(gi, gj, pl.storm_on1, sx1, sy1) : rr1_u;
             hraw = ho - dt2 * ((us - un) / dx + (ve - vw) / dy - ql - rr * pct + evapo);
             hv = fmax(hraw, Real(0.00));
         }
@@ -660,42 +802,87 @@ __global__ void __launch_bounds__(NT)
         }
     }
 
-    // ---- block reductions and one atomic per quantity ----------------------
-    double vals[B_N + 1] = {(double)b_rain, (double)b_src, (double)b_ev, (double)b_out, (double)b_clamp, (double)cm};
+    // ---- block reductions (working precision), one atomic per quantity ----
+    Real vals[B_N + 1] = {b_rain, b_src, b_ev, b_out, b_clamp, cm};
     const int lane = tid & 31, wid = tid >> 5;
 #pragma unroll
     for (int q = 0; q < B_N; q++) {
-        double v = vals[q];
+        Real v = vals[q];
+#pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         vals[q] = v;
     }
     {
-        double v = vals[B_N];
+        Real v = vals[B_N];
+#pragma unroll
         for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
         vals[B_N] = v;
     }
     const bool any_bad = __syncthreads_or(bad);
-    if (lane == 0)
+    if (lane == 0) {
+#pragma unroll
         for (int q = 0; q <= B_N; q++) s_red[wid][q] = vals[q];
-    __syncthreads();
-    if (tid == 0) {
-        double acc[B_N + 1];
-        for (int q = 0; q <= B_N; q++) acc[q] = s_red[0][q];
-        for (int w = 1; w < NW; w++) {
-            for (int q = 0; q < B_N; q++) acc[q] += s_red[w][q];
-            acc[B_N] = fmax(acc[B_N], s_red[w][B_N]);
-        }
-        Clock &co = clk[slot_out];
-        const double area = G.dx * G.dy;
-        const double scale = dt2d * area;
-        if (acc[B_RAIN] != 0.0) atomicAdd(&co.step[B_RAIN], acc[B_RAIN] * scale);
-        if (acc[B_SRC] != 0.0) atomicAdd(&co.step[B_SRC], acc[B_SRC] * scale);
-        if (acc[B_EV] != 0.0) atomicAdd(&co.step[B_EV], acc[B_EV] * scale);
-        if (acc[B_OUT] != 0.0) atomicAdd(&co.step[B_OUT], acc[B_OUT] * dt2d * G.dy);
-        if (acc[B_CLAMP] != 0.0) atomicAdd(&co.step[B_CLAMP], acc[B_CLAMP] * area);
-        if (acc[B_N] > 0.0) atomicMax(&co.cmax_bits, (unsigned long long)__double_as_longlong(acc[B_N]));
-        if (any_bad) atomicOr(&co.nonfinite, 1u);
     }
+    __syncthreads();
+    if (tid != 0) return;
+    Real acc[B_N + 1];
+#pragma unroll
+    for (int q = 0; q <= B_N; q++) acc[q] = s_red[0][q];
+    for (int w = 1; w < NW; w++) {
+#pragma unroll
+        for (int q = 0; q < B_N; q++) acc[q] += s_red[w][q];
+        acc[B_N] = fmax(acc[B_N], s_red[w][B_N]);
+    }
+    Clock &co = clk[slot_out];
+    const double area = G.dx * G.dy;
+    const double scale = pl.d.dt2 * area;
+    if (acc[B_RAIN] != Real(0)) atomicAdd(&co.step[B_RAIN], (double)acc[B_RAIN] * scale);
+    if (acc[B_SRC] != Real(0)) atomicAdd(&co.step[B_SRC], (double)acc[B_SRC] * scale);
+    if (acc[B_EV] != Real(0)) atomicAdd(&co.step[B_EV], (double)acc[B_EV] * scale);
+    if (acc[B_OUT] != Real(0)) atomicAdd(&co.step[B_OUT], (double)acc[B_OUT] * pl.d.dt2 * G.dy);
+    if (acc[B_CLAMP] != Real(0)) atomicAdd(&co.step[B_CLAMP], (double)acc[B_CLAMP] * area);
+    if (acc[B_N] > Real(0))
+        atomicMax(&co.cmax_bits, (unsigned long long)__double_as_longlong((double)acc[B_N]));
+    if (any_bad) atomicOr(&co.nonfinite, 1u);
+
+    // ---- the last CTA to finish finalises the slot and plans the next launch
+    __threadfence();
+    const unsigned int ticket = atomicAdd(&co.done_blocks, 1u);
+    if (ticket != gridDim.x - 1) return;
+    __threadfence();
+    volatile Clock *cov = &co;
+    const unsigned long long cmax_new = cov->cmax_bits;
+    const double t_new = (pl.t0 + pl.dt) + pl.dt;  // cu:1297, cu:1335
+    const long long steps_new = ci.steps + 1;
+    for (int k = 0; k < B_N; k++) {  // fold the previous iteration's sums (Kahan)
+        double s = ci.tot_s[k], c = ci.tot_c[k];
+        double y = ci.step[k] - c;
+        double tt = s + y;
+        co.tot_c[k] = (tt - s) - y;
+        co.tot_s[k] = tt;
+    }
+    co.t = t_new;
+    co.dt = pl.dt;
+    co.steps = steps_new;
+    co.buf = 1 - ci.buf;
+    co.ran = 1;
+    co.nonfinite = cov->nonfinite | ci.nonfinite;
+    co.status = cov->status | ci.status;
+    co.plan = make_plan(t_new, cmax_new, steps_new, *ctl, G, F);
+    Clock &cn = clk[slot_nx];
+    cn.cmax_bits = 0ull;
+    cn.nonfinite = 0u;
+    cn.status = 0u;
+    cn.done_blocks = 0u;
+    for (int k = 0; k < B_N; k++) cn.step[k] = 0.0;
+}
+
+// Plans the launch that will read slot `slot` (used when a run starts or its
+// control changes).  One thread.
+static __global__ void plan_kernel(const GridDesc G, const ForcingDesc F, Clock *__restrict__ clk,
+                            const Control *__restrict__ ctl, const int slot) {
+    Clock &c = clk[slot];
+    c.plan = make_plan(c.t, c.cmax_bits, c.steps, *ctl, G, F);
 }
 
 }  // namespace sw2d

@@ -21,8 +21,12 @@ inline int grid_for(long long n, int threads) {
 template <class Real, int TH, int TW, int NT>
 cudaError_t step_prepare() {
     constexpr size_t smem = step_smem_bytes<Real, TH, TW>();
-    return cudaFuncSetAttribute(step_kernel<Real, TH, TW, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(step_kernel<Real, TH, TW, NT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    // all of the unified L1/shared storage as shared memory: more resident CTAs
+    return cudaFuncSetAttribute(step_kernel<Real, TH, TW, NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                (int)cudaSharedmemCarveoutMaxShared);
 }
 
 template <class Real, int TH, int TW, int NT>

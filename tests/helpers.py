@@ -23,7 +23,8 @@ def make_pair(O, sw2d, rows, cols, dx, z, h0, n=None, manning=0.0, precision=0, 
 
 def set_forcing(O, o, g, rain_kind=0, rain=None, rain_dt=1.0, storm=None, ev=None, ev_dt=1.0,
                 sources=None, src_q=None, dtoq=1.0):
-    o.set_forcing(O.OracleForcing(rain_kind=rain_kind, rain=rain, rain_dt=rain_dt, storm=storm, ev=ev,
+    kind = O.RAIN_STORM if storm is not None else rain_kind
+    o.set_forcing(O.OracleForcing(rain_kind=kind, rain=rain, rain_dt=rain_dt, storm=storm, ev=ev,
                                   ev_dt=ev_dt, sources=sources, src_q=src_q, dtoq=dtoq))
     if storm is not None:
         g.set_storm(storm["peak"], storm["x0"], storm["y0"], storm["vx"], storm["vy"], storm["sigma"],
