@@ -53,6 +53,11 @@ enum { SW2D_PREC_F64 = 0, SW2D_PREC_F32 = 1 };
  *        of the current state. */
 enum { SW2D_DT_FIXED = 0, SW2D_DT_CFL = 1 };
 
+/* Step kernels.  TILE: one CTA per 2-D tile staged in shared memory (the
+ * FP64 path).  STREAM: one warp per 25-column strip marching down the rows
+ * with a register pipeline (FP32 only).  AUTO: TILE for FP64, STREAM for FP32. */
+enum { SW2D_KERNEL_AUTO = 0, SW2D_KERNEL_TILE = 1, SW2D_KERNEL_STREAM = 2 };
+
 enum {
     SW2D_FIELD_DEPTH = 0,     /* h, rows x cols            (reference d_h)   */
     SW2D_FIELD_UM = 1,        /* x-face discharge, (rows+1) x cols (d_um)   */
@@ -86,8 +91,10 @@ typedef struct {
     double cfl;             /* Courant number for SW2D_DT_CFL (0.5) */
     int32_t south_open;     /* 1: free outfall through the south edge (extension) */
     int32_t device;         /* CUDA device ordinal */
-    int32_t tile_h, tile_w; /* core tile of the step kernel, 0 = default */
-    int32_t reserved[4];
+    int32_t tile_h, tile_w; /* core tile of the shared-memory step kernel, 0 = default */
+    int32_t kernel;         /* SW2D_KERNEL_*: which step kernel (AUTO picks per precision) */
+    int32_t strip_h;        /* rows per warp of the FP32 streaming kernel, 0 = auto */
+    int32_t reserved[2];
 } sw2d_config;
 
 typedef struct {

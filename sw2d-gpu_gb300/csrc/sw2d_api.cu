@@ -37,6 +37,8 @@ struct sw2d_handle {
     int pitch = 0;
     size_t plane = 0;  // elements per pitched array: (rows+1) * pitch
     int tile_h = 16, tile_w = 32, nblocks = 0;
+    bool stream_kernel = false;  // FP32 warp-streaming kernel instead of the tile kernel
+    int strip_h = 0, stream_tiles_w = 0, stream_units = 0;
     cudaStream_t stream = nullptr;
     void *h[2] = {nullptr, nullptr}, *um[2] = {nullptr, nullptr}, *vn[2] = {nullptr, nullptr};
     void *z = nullptr, *nman = nullptr;
@@ -121,6 +123,9 @@ StateBufs<Real> make_bufs(const sw2d_handle *h) {
 }
 
 cudaError_t launch_one(sw2d_handle *h, int slot) {
+    if (h->stream_kernel)
+        return launch_stream_step(h->nblocks, h->stream_tiles_w, h->strip_h, h->stream_units, h->G, h->F,
+                                  make_bufs<float>(h), make_thr<float>(h->cfg), h->d_clk, h->d_ctl, slot, h->stream);
     if (is_f64(h))
         return launch_step(h->tile_h, h->tile_w, h->nblocks, h->G, h->F, make_bufs<double>(h),
                            make_thr<double>(h->cfg), h->d_clk, h->d_ctl, slot, h->stream);
@@ -138,6 +143,10 @@ int validate(const sw2d_config *c, std::string *why) {
     if (c->dt_mode != SW2D_DT_FIXED && c->dt_mode != SW2D_DT_CFL) return *why = "unknown dt_mode", 0;
     if (c->dt_mode == SW2D_DT_CFL && !(c->cfl > 0)) return *why = "cfl must be > 0", 0;
     if (!(c->g > 0) || !(c->th >= 0)) return *why = "g must be > 0 and th >= 0", 0;
+    if (c->kernel < SW2D_KERNEL_AUTO || c->kernel > SW2D_KERNEL_STREAM) return *why = "unknown kernel", 0;
+    if (c->kernel == SW2D_KERNEL_STREAM && c->precision != SW2D_PREC_F32)
+        return *why = "the streaming kernel is FP32 only", 0;
+    if (c->strip_h < 0) return *why = "strip_h must be >= 0", 0;
     return 1;
 }
 
@@ -293,7 +302,12 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
     if (cudaMallocHost((void **)&h->h_ctl, sizeof(Control)) != cudaSuccess) return bail(SW2D_ERR_OOM);
     if (cudaMallocHost((void **)&h->h_partial, kVolumeBlocks * sizeof(double)) != cudaSuccess) return bail(SW2D_ERR_OOM);
     if (cudaMemset(h->d_clk, 0, 3 * sizeof(Clock)) != cudaSuccess) return bail(SW2D_ERR_CUDA);
-    e = is_f64(h) ? prepare_step(h->tile_h, h->tile_w, 0.0) : prepare_step(h->tile_h, h->tile_w, 0.0f);
+    h->stream_kernel = cfg->precision == SW2D_PREC_F32 && cfg->kernel != SW2D_KERNEL_TILE;
+    if (h->stream_kernel) {
+        e = prepare_stream_step();
+    } else {
+        e = is_f64(h) ? prepare_step(h->tile_h, h->tile_w, 0.0) : prepare_step(h->tile_h, h->tile_w, 0.0f);
+    }
     if (e != cudaSuccess) return bail(SW2D_ERR_CUDA);
 
     GridDesc &G = h->G;
@@ -303,6 +317,26 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
     G.tiles_w = (cfg->cols + h->tile_w - 1) / h->tile_w;
     const int tiles_h = (cfg->rows + h->tile_h - 1) / h->tile_h;
     h->nblocks = tiles_h * G.tiles_w;
+    if (h->stream_kernel) {
+        const int oc = stream_out_cols();
+        h->stream_tiles_w = (cfg->cols + oc - 1) / oc;
+        int sh = cfg->strip_h;
+        if (sh <= 0) {  // tallest strip that still fills the GPU with about one wave of warps
+            int dev_sms = 0;
+            cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, cfg->device);
+            const long long want = (long long)(dev_sms > 0 ? dev_sms : 152) * 20;
+            const int cand[] = {128, 96, 64, 48, 32, 24, 16};
+            sh = 16;
+            for (int c : cand)
+                if ((long long)h->stream_tiles_w * ((cfg->rows + c - 1) / c) >= want) {
+                    sh = c;
+                    break;
+                }
+        }
+        h->strip_h = sh;
+        h->stream_units = h->stream_tiles_w * ((cfg->rows + sh - 1) / sh);
+        h->nblocks = (h->stream_units + kStreamWarps - 1) / kStreamWarps;
+    }
     G.dt_mode = cfg->dt_mode;
     G.south_open = cfg->south_open ? 1 : 0;
     G.n_src = 0;

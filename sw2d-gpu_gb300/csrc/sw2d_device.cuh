@@ -45,6 +45,7 @@ enum { B_RAIN = 0, B_SRC = 1, B_EV = 2, B_OUT = 3, B_CLAMP = 4, B_N = 5 };
 enum { ST_TOO_MANY_LOCAL_SOURCES = 1 };
 
 constexpr int kMaxLocalSources = 64;
+constexpr int kBuckets = 16;
 
 // What one launch does, computed once per launch (never per thread: FP64
 // arithmetic runs at a small fraction of the FP32 rate on this GPU).
@@ -82,6 +83,11 @@ struct __align__(16) Clock {
     unsigned int done_blocks;      // CTAs of the writing launch that have finished
     unsigned int pad;
     Plan plan;                     // what the launch reading this slot does
+    // accumulators of the writing launch, spread over kBuckets addresses so
+    // that thousands of CTAs do not serialise on one atomic location; summed
+    // in bucket order by the last CTA
+    double stepb[B_N][kBuckets];
+    unsigned long long cmaxb[kBuckets];
 };
 
 struct Control {
@@ -279,6 +285,92 @@ __device__ inline Plan make_plan(double t, unsigned long long cmax_bits, long lo
 }
 
 // ---------------------------------------------------------------------------
+// clock-slot bookkeeping shared by the step kernels
+// ---------------------------------------------------------------------------
+__device__ inline void clear_slot_accumulators(Clock &c) {
+    c.cmax_bits = 0ull;
+    c.nonfinite = 0u;
+    c.status = 0u;
+    c.done_blocks = 0u;
+    for (int k = 0; k < B_N; k++) {
+        c.step[k] = 0.0;
+        for (int b = 0; b < kBuckets; b++) c.stepb[k][b] = 0.0;
+    }
+    for (int b = 0; b < kBuckets; b++) c.cmaxb[b] = 0ull;
+}
+
+__device__ inline void fold_totals(const Clock &ci, Clock &co) {
+    for (int k = 0; k < B_N; k++) {  // Kahan: running total += previous iteration's sum
+        double s = ci.tot_s[k], c = ci.tot_c[k];
+        double y = ci.step[k] - c;
+        double tt = s + y;
+        co.tot_c[k] = (tt - s) - y;
+        co.tot_s[k] = tt;
+    }
+}
+
+// A launch whose plan says "do not run": one thread carries the state's
+// clock to the next slot unchanged.
+__device__ inline void carry_slot(const Clock &ci, Clock &co, Clock &cn) {
+    fold_totals(ci, co);
+    co.t = ci.t;
+    co.dt = ci.dt;
+    co.steps = ci.steps;
+    co.buf = ci.buf;
+    co.ran = 0;
+    co.cmax_bits = ci.cmax_bits;
+    co.nonfinite = ci.nonfinite;
+    co.status = ci.status;
+    co.plan = ci.plan;
+    for (int k = 0; k < B_N; k++) co.step[k] = 0.0;
+    clear_slot_accumulators(cn);
+}
+
+// One CTA's contribution (one thread calls it): budget sums [m^3 already
+// scaled], CFL bound, non-finite flag.
+__device__ inline void accumulate_slot(Clock &co, int bucket, const double v[B_N], double cmax, bool bad) {
+    for (int k = 0; k < B_N; k++)
+        if (v[k] != 0.0) atomicAdd(&co.stepb[k][bucket], v[k]);
+    if (cmax > 0.0) atomicMax(&co.cmaxb[bucket], (unsigned long long)__double_as_longlong(cmax));
+    if (bad) atomicOr(&co.nonfinite, 1u);
+}
+
+// Called by one thread of every CTA after its accumulate_slot; the last CTA
+// of the launch finalises slot `co` (time, budgets, CFL bound, plan of the
+// next launch) and clears slot `cn` for the next launch.  No CTA waits.
+__device__ inline void finish_cta(const Clock &ci, Clock &co, Clock &cn, const Plan &pl, const Control &ctl,
+                                  const GridDesc &G, const ForcingDesc &F) {
+    __threadfence();
+    const unsigned int ticket = atomicAdd(&co.done_blocks, 1u);
+    if (ticket != gridDim.x * gridDim.y - 1) return;
+    __threadfence();
+    volatile Clock *cov = &co;
+    unsigned long long cm = 0ull;
+    for (int b = 0; b < kBuckets; b++) {
+        const unsigned long long v = cov->cmaxb[b];
+        cm = v > cm ? v : cm;
+    }
+    for (int k = 0; k < B_N; k++) {
+        double sum = 0.0;
+        for (int b = 0; b < kBuckets; b++) sum += cov->stepb[k][b];
+        co.step[k] = sum;
+    }
+    const double t_new = (pl.t0 + pl.dt) + pl.dt;  // cu:1297, cu:1335
+    const long long steps_new = ci.steps + 1;
+    fold_totals(ci, co);
+    co.cmax_bits = cm;
+    co.t = t_new;
+    co.dt = pl.dt;
+    co.steps = steps_new;
+    co.buf = 1 - ci.buf;
+    co.ran = 1;
+    co.nonfinite = cov->nonfinite | ci.nonfinite;
+    co.status = cov->status | ci.status;
+    co.plan = make_plan(t_new, cm, steps_new, ctl, G, F);
+    clear_slot_accumulators(cn);
+}
+
+// ---------------------------------------------------------------------------
 // deterministic FP64 log / exp / power.  Same algorithm and operation order
 // as the oracle's (log: atanh series on m in [1/sqrt2, sqrt2); exp:
 // Cody-Waite reduction by ln2 split into a 21-bit head and a tail, Taylor
@@ -442,31 +534,7 @@ __global__ void __launch_bounds__(NT)
     const Plan pl = ci.plan;
 
     if (!pl.run) {  // nothing to do: carry the state's clock forward
-        if (blockIdx.x == 0 && tid == 0) {
-            Clock &co = clk[slot_out];
-            for (int k = 0; k < B_N; k++) {
-                double s = ci.tot_s[k], c = ci.tot_c[k];
-                double y = ci.step[k] - c;
-                double tt = s + y;
-                co.tot_c[k] = (tt - s) - y;
-                co.tot_s[k] = tt;
-            }
-            co.t = ci.t;
-            co.dt = ci.dt;
-            co.steps = ci.steps;
-            co.buf = ci.buf;
-            co.ran = 0;
-            co.cmax_bits = ci.cmax_bits;
-            co.nonfinite = ci.nonfinite;
-            co.status = ci.status;
-            co.plan = pl;
-            Clock &cn = clk[slot_nx];
-            cn.cmax_bits = 0ull;
-            cn.nonfinite = 0u;
-            cn.status = 0u;
-            cn.done_blocks = 0u;
-            for (int k = 0; k < B_N; k++) cn.step[k] = 0.0;
-        }
+        if (blockIdx.x == 0 && tid == 0) carry_slot(ci, clk[slot_out], clk[slot_nx]);
         return;
     }
 
@@ -833,48 +901,16 @@ __global__ void __launch_bounds__(NT)
         for (int q = 0; q < B_N; q++) acc[q] += s_red[w][q];
         acc[B_N] = fmax(acc[B_N], s_red[w][B_N]);
     }
-    Clock &co = clk[slot_out];
     const double area = G.dx * G.dy;
     const double scale = pl.d.dt2 * area;
-    if (acc[B_RAIN] != Real(0)) atomicAdd(&co.step[B_RAIN], (double)acc[B_RAIN] * scale);
-    if (acc[B_SRC] != Real(0)) atomicAdd(&co.step[B_SRC], (double)acc[B_SRC] * scale);
-    if (acc[B_EV] != Real(0)) atomicAdd(&co.step[B_EV], (double)acc[B_EV] * scale);
-    if (acc[B_OUT] != Real(0)) atomicAdd(&co.step[B_OUT], (double)acc[B_OUT] * pl.d.dt2 * G.dy);
-    if (acc[B_CLAMP] != Real(0)) atomicAdd(&co.step[B_CLAMP], (double)acc[B_CLAMP] * area);
-    if (acc[B_N] > Real(0))
-        atomicMax(&co.cmax_bits, (unsigned long long)__double_as_longlong((double)acc[B_N]));
-    if (any_bad) atomicOr(&co.nonfinite, 1u);
-
-    // ---- the last CTA to finish finalises the slot and plans the next launch
-    __threadfence();
-    const unsigned int ticket = atomicAdd(&co.done_blocks, 1u);
-    if (ticket != gridDim.x - 1) return;
-    __threadfence();
-    volatile Clock *cov = &co;
-    const unsigned long long cmax_new = cov->cmax_bits;
-    const double t_new = (pl.t0 + pl.dt) + pl.dt;  // cu:1297, cu:1335
-    const long long steps_new = ci.steps + 1;
-    for (int k = 0; k < B_N; k++) {  // fold the previous iteration's sums (Kahan)
-        double s = ci.tot_s[k], c = ci.tot_c[k];
-        double y = ci.step[k] - c;
-        double tt = s + y;
-        co.tot_c[k] = (tt - s) - y;
-        co.tot_s[k] = tt;
-    }
-    co.t = t_new;
-    co.dt = pl.dt;
-    co.steps = steps_new;
-    co.buf = 1 - ci.buf;
-    co.ran = 1;
-    co.nonfinite = cov->nonfinite | ci.nonfinite;
-    co.status = cov->status | ci.status;
-    co.plan = make_plan(t_new, cmax_new, steps_new, *ctl, G, F);
-    Clock &cn = clk[slot_nx];
-    cn.cmax_bits = 0ull;
-    cn.nonfinite = 0u;
-    cn.status = 0u;
-    cn.done_blocks = 0u;
-    for (int k = 0; k < B_N; k++) cn.step[k] = 0.0;
+    double v[B_N];
+    v[B_RAIN] = (double)acc[B_RAIN] * scale;
+    v[B_SRC] = (double)acc[B_SRC] * scale;
+    v[B_EV] = (double)acc[B_EV] * scale;
+    v[B_OUT] = (double)acc[B_OUT] * pl.d.dt2 * G.dy;
+    v[B_CLAMP] = (double)acc[B_CLAMP] * area;
+    accumulate_slot(clk[slot_out], blockIdx.x % kBuckets, v, (double)acc[B_N], any_bad);
+    finish_cta(ci, clk[slot_out], clk[slot_nx], pl, *ctl, G, F);
 }
 
 // Plans the launch that will read slot `slot` (used when a run starts or its

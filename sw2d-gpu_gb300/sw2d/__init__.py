@@ -5,7 +5,7 @@ work runs in hand-written sm_103a CUDA kernels; this package only binds the
 ABI, builds synthetic scenarios and drives runs.
 """
 from .native import (  # noqa: F401
-    DT_CFL, DT_FIXED, FIELD_DEPTH, FIELD_ELEVATION, FIELD_UM, FIELD_UU, FIELD_VN, FIELD_VV,
+    DT_CFL, DT_FIXED, KERNEL_AUTO, KERNEL_STREAM, KERNEL_TILE, FIELD_DEPTH, FIELD_ELEVATION, FIELD_UM, FIELD_UU, FIELD_VN, FIELD_VV,
     PREC_F32, PREC_F64, RAIN_COMPAT, RAIN_LINEAR, RAIN_NONE, RAIN_STEP, RAIN_STORM,
     Config, SW2DError, Solver, default_config, device_bytes, load,
 )

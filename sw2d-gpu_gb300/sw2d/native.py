@@ -20,6 +20,7 @@ PREC_F64, PREC_F32 = 0, 1
 DT_FIXED, DT_CFL = 0, 1
 FIELD_DEPTH, FIELD_UM, FIELD_VN, FIELD_UU, FIELD_VV, FIELD_ELEVATION = range(6)
 RAIN_NONE, RAIN_COMPAT, RAIN_STEP, RAIN_LINEAR, RAIN_STORM = range(5)
+KERNEL_AUTO, KERNEL_TILE, KERNEL_STREAM = range(3)
 
 
 class Config(C.Structure):
@@ -32,7 +33,8 @@ class Config(C.Structure):
         ("dt", C.c_double), ("cfl", C.c_double),
         ("south_open", C.c_int32), ("device", C.c_int32),
         ("tile_h", C.c_int32), ("tile_w", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("kernel", C.c_int32), ("strip_h", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 

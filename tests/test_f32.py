@@ -1,0 +1,139 @@
+"""FP32 paths (warp-streaming kernel, shared-memory tile kernel) against the
+FP64 oracle and against each other, through the C ABI.
+
+Stated bounds for the FP32 state: max |dh| <= 1 mm against the FP64 oracle
+and flooded area (h > th) within 0.1 %, on rain-runoff scenarios; the
+relative volume-conservation error of the FP64 budget <= 1e-6.
+"""
+import numpy as np
+import pytest
+
+from helpers import make_pair, max_abs, set_forcing
+
+pytestmark = pytest.mark.gpu
+
+TH = 1.0e-4
+TOL_MM = 1.0e-3
+
+
+def _f32(sw2d, rows, cols, dx, z, h0, n=None, kernel=0, strip_h=0, **kw):
+    g = sw2d.Solver(rows=rows, cols=cols, dx=dx, dy=dx, precision=sw2d.PREC_F32, kernel=kernel, strip_h=strip_h,
+                    **kw)
+    g.set_static(z, n)
+    g.set_state(h0)
+    return g
+
+
+def _catchment(seed=3, rows=96, cols=80, holes=True):
+    from sw2d import scenarios as S
+    s = S.catchment(rows, dx=5.0, seed=seed, cols=cols)
+    z = s["z"].copy()
+    if holes:
+        rng = np.random.default_rng(seed)
+        z[rng.random(z.shape) < 0.02] = -9999.0
+    return s, z
+
+
+def _flooded_area_rel(a, b):
+    na, nb = np.count_nonzero(a > TH), np.count_nonzero(b > TH)
+    return abs(na - nb) / max(na, 1)
+
+
+@pytest.mark.parametrize("kernel", [1, 2])
+def test_f32_catchment_rain_vs_oracle(oracle_mod, sw2d_mod, kernel):
+    s, z = _catchment()
+    o, g64 = make_pair(oracle_mod, sw2d_mod, 96, 80, 5.0, z, s["h0"], n=s["n"], south_open=1, dt_mode=1, dt=2.0)
+    g64.close()
+    g = _f32(sw2d_mod, 96, 80, 5.0, z, s["h0"], n=s["n"], kernel=kernel, south_open=1, dt_mode=1, dt=2.0)
+    set_forcing(oracle_mod, o, g, rain_kind=2, rain=np.array([100.0, 50.0]), rain_dt=600.0)
+    o.advance(10 ** 6, t_end=1200.0)
+    g.advance(10 ** 6, t_end=1200.0)
+    a, b = o.state()["h"], g.depth()
+    err = max_abs(a, b)
+    print("max |dh| =", err, "flooded-area rel diff =", _flooded_area_rel(a, b))
+    assert err <= TOL_MM
+    assert _flooded_area_rel(a, b) <= 1e-3
+    bud = g.budget()
+    rhs = bud["volume0"] + bud["rain_in"] + bud["source_in"] - bud["evap_out"] - bud["outflow"] + bud["clamp_gain"]
+    vol_err = abs(bud["volume"] - rhs) / bud["volume"]
+    print("relative volume error", vol_err)
+    assert vol_err <= 1e-6
+
+
+def test_stream_matches_tile_kernel(sw2d_mod):
+    """Same scheme, same precision, two kernel organisations."""
+    s, z = _catchment(seed=4, rows=70, cols=130)
+    g1 = _f32(sw2d_mod, 70, 130, 5.0, z, s["h0"], n=s["n"], kernel=1, south_open=1, dt_mode=1, dt=2.0)
+    g2 = _f32(sw2d_mod, 70, 130, 5.0, z, s["h0"], n=s["n"], kernel=2, south_open=1, dt_mode=1, dt=2.0, strip_h=16)
+    for g in (g1, g2):
+        g.set_rain(sw2d_mod.RAIN_STEP, [150.0], 3600.0)
+        assert g.advance(300) == 300
+    b1, b2 = g1.budget(), g2.budget()
+    assert abs(b1["t"] - b2["t"]) <= 1e-6 * b1["t"]
+    assert max_abs(g1.depth(), g2.depth()) <= 1e-4
+
+
+@pytest.mark.parametrize("strip_h", [1, 7, 16, 64, 128])
+def test_stream_strip_heights_agree(sw2d_mod, strip_h):
+    """The strip decomposition must not change the result (up to FP32
+    contraction differences, there are none: same code per cell)."""
+    s, z = _catchment(seed=6, rows=50, cols=60)
+    ref = _f32(sw2d_mod, 50, 60, 5.0, z, s["h0"], n=s["n"], kernel=2, strip_h=50, dt_mode=1, dt=2.0)
+    g = _f32(sw2d_mod, 50, 60, 5.0, z, s["h0"], n=s["n"], kernel=2, strip_h=strip_h, dt_mode=1, dt=2.0)
+    for x in (ref, g):
+        x.set_rain(sw2d_mod.RAIN_STEP, [200.0], 3600.0)
+        x.advance(120)
+    assert np.array_equal(ref.depth(), g.depth())
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (1, 9), (9, 1), (17, 33), (33, 17), (3, 65), (40, 26), (5, 50)])
+def test_stream_ragged_grids_vs_oracle(oracle_mod, sw2d_mod, shape):
+    rows, cols = shape
+    rng = np.random.default_rng(rows * 100 + cols)
+    z = rng.uniform(0, 0.5, (rows, cols))
+    h0 = rng.uniform(0, 1.0, (rows, cols)) * (rng.random((rows, cols)) < 0.6)
+    o = oracle_mod.Oracle(rows, cols, 1.0, 1.0, z, dt_mode=0, dt=0.02)
+    o.set_state(h0)
+    g = _f32(sw2d_mod, rows, cols, 1.0, z, h0, kernel=2, dt_mode=0, dt=0.02)
+    o.advance(40, 1e9)
+    g.advance(40, 1e9)
+    assert max_abs(o.state()["h"], g.depth()) <= TOL_MM
+
+
+def test_stream_sources_storm_open_south(oracle_mod, sw2d_mod):
+    from sw2d import scenarios as S
+    rows, cols = 64, 72
+    s = S.catchment(rows, dx=20.0, seed=13, cols=cols, manning=0.05)
+    o, g64 = make_pair(oracle_mod, sw2d_mod, rows, cols, 20.0, s["z"], s["h0"], manning=0.05, south_open=1,
+                       dt_mode=1, dt=5.0)
+    g64.close()
+    g = _f32(sw2d_mod, rows, cols, 20.0, s["z"], s["h0"], manning=0.05, kernel=2, south_open=1, dt_mode=1, dt=5.0)
+    storm = {"peak": 200.0, "x0": 0.0, "y0": 0.0, "vx": 1.5, "vy": 1.0, "sigma": 400.0}
+    cells = np.array([10 * cols + 30, 40 * cols + 5, 40 * cols + 5], dtype=np.int32)
+    q = np.array([[2.0, 1.0, 3.0], [4.0, 0.5, 1.0], [1.0, 0.0, 0.0], [0.0, 0.0, 0.0]])
+    set_forcing(oracle_mod, o, g, storm=storm, sources=cells, src_q=q, dtoq=200.0)
+    o.advance(10 ** 6, t_end=600.0)
+    g.advance(10 ** 6, t_end=600.0)
+    a, b = o.state()["h"], g.depth()
+    print("max |dh| =", max_abs(a, b))
+    assert max_abs(a, b) <= TOL_MM
+    bo, bg = o.budget(), g.budget()
+    assert bg["source_in"] == pytest.approx(bo["source_in"], rel=1e-4)
+    assert bg["rain_in"] == pytest.approx(bo["rain_in"], rel=1e-4)
+    assert bg["outflow"] == pytest.approx(bo["outflow"], rel=1e-3, abs=1e-3)
+
+
+def test_f32_dam_break_front(oracle_mod, sw2d_mod):
+    """A frictionless dam break is a moving discontinuity: FP32 and FP64
+    agree on volume and on the front position within one cell."""
+    from sw2d import scenarios as S
+    s = S.dam_break_channel(64, 256, 1.0, x_gate=100.0)
+    o = oracle_mod.Oracle(64, 256, 1.0, 1.0, s["z"], dt_mode=1, dt=1.0)
+    o.set_state(s["h0"])
+    g = _f32(sw2d_mod, 64, 256, 1.0, s["z"], s["h0"], kernel=2, dt_mode=1, dt=1.0)
+    o.advance(400)
+    g.advance(400)
+    a, b = o.state()["h"], g.depth()
+    front = lambda h: int(np.max(np.nonzero(h[32] > 1e-3)[0]))
+    assert abs(front(a) - front(b)) <= 1
+    assert g.budget()["volume"] == pytest.approx(o.volume(), rel=1e-6)
