@@ -94,7 +94,9 @@ typedef struct {
     int32_t tile_h, tile_w; /* core tile of the shared-memory step kernel, 0 = default */
     int32_t kernel;         /* SW2D_KERNEL_*: which step kernel (AUTO picks per precision) */
     int32_t strip_h;        /* rows per warp of the FP32 streaming kernel, 0 = auto */
-    int32_t reserved[2];
+    int32_t variant;        /* streaming-kernel build (occupancy / unrolling), 0 = default;
+                               chosen by the autotuner */
+    int32_t reserved[1];
 } sw2d_config;
 
 typedef struct {

@@ -25,12 +25,31 @@ cudaError_t launch_step(int th, int tw, int nblocks, const GridDesc &G, const Fo
 
 int stream_out_cols() { return kStreamOut; }
 
-cudaError_t prepare_stream_step() {
-    return cudaFuncSetAttribute(stream_step_kernel<kStreamWarps>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                (int)cudaSharedmemCarveoutMaxL1);
+// Builds of the streaming kernel the autotuner chooses from:
+// (warps per CTA, minimum resident CTAs per SM for the register budget, row-loop unrolling).
+#define SW2D_STREAM_VARIANTS(X) X(0, 4, 4, 1) X(1, 4, 1, 1) X(2, 4, 5, 1) X(3, 4, 6, 1) X(4, 4, 4, 2) X(5, 8, 2, 1)
+
+int stream_variants() { return 6; }
+
+int stream_warps(int variant) {
+#define SW2D_W(id, nw, mb, un) \
+    if (variant == id) return nw;
+    SW2D_STREAM_VARIANTS(SW2D_W)
+#undef SW2D_W
+    return 4;
 }
 
-cudaError_t launch_stream_step(int nblocks, int tiles_w, int strip_h, int units, const GridDesc &G,
+cudaError_t prepare_stream_step(int variant) {
+#define SW2D_P(id, nw, mb, un)                                                                               \
+    if (variant == id)                                                                                      \
+        return cudaFuncSetAttribute(stream_step_kernel<nw, mb, un>, cudaFuncAttributePreferredSharedMemoryCarveout, \
+                                    (int)cudaSharedmemCarveoutMaxL1);
+    SW2D_STREAM_VARIANTS(SW2D_P)
+#undef SW2D_P
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_h, int units, const GridDesc &G,
                                const ForcingDesc &F, const StateBufs<float> &S, const Thr<float> &T, Clock *clk,
                                const Control *ctl, int slot, cudaStream_t st) {
     StreamShape sh;
@@ -38,8 +57,14 @@ cudaError_t launch_stream_step(int nblocks, int tiles_w, int strip_h, int units,
     sh.strip_h = strip_h;
     sh.units = units;
     sh.pad = 0;
-    stream_step_kernel<kStreamWarps><<<nblocks, kStreamWarps * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh);
-    return cudaGetLastError();
+#define SW2D_L(id, nw, mb, un)                                                                   \
+    if (variant == id) {                                                                         \
+        stream_step_kernel<nw, mb, un><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh); \
+        return cudaGetLastError();                                                               \
+    }
+    SW2D_STREAM_VARIANTS(SW2D_L)
+#undef SW2D_L
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace sw2d

@@ -38,7 +38,7 @@ struct sw2d_handle {
     size_t plane = 0;  // elements per pitched array: (rows+1) * pitch
     int tile_h = 16, tile_w = 32, nblocks = 0;
     bool stream_kernel = false;  // FP32 warp-streaming kernel instead of the tile kernel
-    int strip_h = 0, stream_tiles_w = 0, stream_units = 0;
+    int strip_h = 0, stream_tiles_w = 0, stream_units = 0, variant = 0;
     cudaStream_t stream = nullptr;
     void *h[2] = {nullptr, nullptr}, *um[2] = {nullptr, nullptr}, *vn[2] = {nullptr, nullptr};
     void *z = nullptr, *nman = nullptr;
@@ -124,7 +124,7 @@ StateBufs<Real> make_bufs(const sw2d_handle *h) {
 
 cudaError_t launch_one(sw2d_handle *h, int slot) {
     if (h->stream_kernel)
-        return launch_stream_step(h->nblocks, h->stream_tiles_w, h->strip_h, h->stream_units, h->G, h->F,
+        return launch_stream_step(h->variant, h->nblocks, h->stream_tiles_w, h->strip_h, h->stream_units, h->G, h->F,
                                   make_bufs<float>(h), make_thr<float>(h->cfg), h->d_clk, h->d_ctl, slot, h->stream);
     if (is_f64(h))
         return launch_step(h->tile_h, h->tile_w, h->nblocks, h->G, h->F, make_bufs<double>(h),
@@ -147,6 +147,7 @@ int validate(const sw2d_config *c, std::string *why) {
     if (c->kernel == SW2D_KERNEL_STREAM && c->precision != SW2D_PREC_F32)
         return *why = "the streaming kernel is FP32 only", 0;
     if (c->strip_h < 0) return *why = "strip_h must be >= 0", 0;
+    if (c->variant < 0 || c->variant >= stream_variants()) return *why = "unknown kernel variant", 0;
     return 1;
 }
 
@@ -190,6 +191,10 @@ int capture_graph(sw2d_handle *h) {
 }
 
 void sync_grid_scalars(GridDesc &G) {
+    G.sd.rdx = 1.0 / G.sd.dx;
+    G.sd.rdy = 1.0 / G.sd.dy;
+    G.sf.rdx = (float)G.sd.rdx;
+    G.sf.rdy = (float)G.sd.rdy;
     G.sf.dx = (float)G.sd.dx;
     G.sf.dy = (float)G.sd.dy;
     G.sf.g = (float)G.sd.g;
@@ -303,8 +308,9 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
     if (cudaMallocHost((void **)&h->h_partial, kVolumeBlocks * sizeof(double)) != cudaSuccess) return bail(SW2D_ERR_OOM);
     if (cudaMemset(h->d_clk, 0, 3 * sizeof(Clock)) != cudaSuccess) return bail(SW2D_ERR_CUDA);
     h->stream_kernel = cfg->precision == SW2D_PREC_F32 && cfg->kernel != SW2D_KERNEL_TILE;
+    h->variant = cfg->variant;
     if (h->stream_kernel) {
-        e = prepare_stream_step();
+        e = prepare_stream_step(h->variant);
     } else {
         e = is_f64(h) ? prepare_step(h->tile_h, h->tile_w, 0.0) : prepare_step(h->tile_h, h->tile_w, 0.0f);
     }
@@ -335,7 +341,8 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
         }
         h->strip_h = sh;
         h->stream_units = h->stream_tiles_w * ((cfg->rows + sh - 1) / sh);
-        h->nblocks = (h->stream_units + kStreamWarps - 1) / kStreamWarps;
+        const int nw = stream_warps(h->variant);
+        h->nblocks = (h->stream_units + nw - 1) / nw;
     }
     G.dt_mode = cfg->dt_mode;
     G.south_open = cfg->south_open ? 1 : 0;

@@ -98,6 +98,7 @@ struct Control {
 template <class Real>
 struct GridScalars {
     Real dx, dy, g, manning;
+    Real rdx, rdy;             // 1/dx, 1/dy (used by the FP32 streaming kernel only)
     Real pct_hi, pct_lo;       // 1 - LWL and 1 - (INT + INF)   (cu:627-634)
     Real storm_amp, storm_2s2; // peak/3.6e6 [m/s] and 2 sigma^2 [m^2]
 };

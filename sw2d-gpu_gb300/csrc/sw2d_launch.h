@@ -39,10 +39,11 @@ SW2D_DECLARE_LAUNCHERS(double)
 SW2D_DECLARE_LAUNCHERS(float)
 
 // FP32 warp-streaming step kernel (step_f32.cu)
-constexpr int kStreamWarps = 4;  // warps per CTA
 int stream_out_cols();
-cudaError_t prepare_stream_step();
-cudaError_t launch_stream_step(int nblocks, int tiles_w, int strip_h, int units, const GridDesc &G,
+int stream_variants();
+int stream_warps(int variant);
+cudaError_t prepare_stream_step(int variant);
+cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_h, int units, const GridDesc &G,
                                const ForcingDesc &F, const StateBufs<float> &S, const Thr<float> &T, Clock *clk,
                                const Control *ctl, int slot, cudaStream_t st);
 
