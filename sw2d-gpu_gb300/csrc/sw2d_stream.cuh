@@ -43,52 +43,6 @@ struct StreamShape {
 __device__ __forceinline__ float shup(float v) { return __shfl_up_sync(0xffffffffu, v, 1); }
 __device__ __forceinline__ float shdn(float v) { return __shfl_down_sync(0xffffffffu, v, 1); }
 
-// One face discharge (x- or y-face, same formulas with the roles of the
-// directions swapped), written without branches so that the two faces of a
-// cell interleave in the instruction stream.  a/b: the low/high-index cells;
-// uc: own-direction face velocity; q*: old discharges (own, forward,
-// backward, and the two transverse neighbours); v*: the velocities used for
-// the upwinded convection.  Returns the new discharge before the dry-cell
-// fix, 0 when the face is closed or both cells are dry.
-struct FaceIn {
-    float ha, hb, za, zb;
-    float qc, qf, qb, qe, qw;      // old discharge: this face, +1/-1 along, +1/-1 across
-    float uf, ub;                  // along-face averaged velocities (forward / backward side)
-    float ve, vw;                  // across-face averaged velocities
-    float ufr;                     // |own face velocity| term partner for friction (along)
-    float vtr;                     // transverse velocity average for friction
-    float rn;                      // face Manning n
-    bool open;                     // both cells active and inside the domain
-    bool across_on;                // transverse convection enabled (not on column/row 0)
-    bool along_on;                 // along convection enabled
-};
-
-__device__ __forceinline__ float face_flux(const FaceIn &I, const Thr<float> &T, float g, float dt2, float dt2d_along,
-                                           float dt2d_across) {
-    const float ha = I.ha, hb = I.hb, za = I.za, zb = I.zb;
-    const bool aw = ha >= T.gt_th, bw = hb >= T.gt_th;
-    const bool ad = !(ha >= T.ge_th), bd = !(hb >= T.ge_th);
-    const float ea = ha + za, eb = hb + zb;
-    // dry-bed rules (cu:130-159)
-    const bool c1 = eb < za;
-    const bool c2 = ea < zb;
-    const bool c3 = (bw && ad) || (bd && aw);
-    const float q1 = aw ? 0.5440f * ha * sqrtf(g * ha) : 0.f;
-    const float q2 = bw ? -0.544f * hb * sqrtf(g * hb) : 0.f;
-    const float hh3 = fmaxf(eb, ea) - fmaxf(zb, za);
-    const float q3 = ((hb > 0.f) || (ha > 0.f)) ? (bw ? -0.350f : 0.350f) * hh3 * sqrtf(2.00f * g * hh3) : 0.f;
-    // momentum (cu:166-203)
-    const float hm = 0.50f * (hb + ha);
-    const float grav = g * hm * dt2d_along * (eb - ha - za);  // cu:166 / cu:283
-    const float conv_along = I.along_on ? dt2d_along * (upwind<float>(I.uf, I.qf, I.qc) - upwind_r<float>(I.ub, I.qb, I.qc)) : 0.f;
-    const float conv_across = I.across_on ? dt2d_across * (upwind<float>(I.ve, I.qe, I.qc) - upwind_r<float>(I.vw, I.qw, I.qc)) : 0.f;
-    float ram = g * I.rn * I.rn * sqrtf(I.ufr * I.ufr + I.vtr * I.vtr) / RT<float>::pow_(hm);
-    ram = ((hm >= T.gt_th) && I.rn != 0.f) ? ram : 0.f;
-    const float qm = ((1.00f - dt2 * ram * 0.50f) * I.qc + (-conv_along - conv_across - grav)) / (1.00f + dt2 * ram * 0.50f);
-    const float q = c1 ? q1 : (c2 ? q2 : (c3 ? q3 : qm));
-    return (I.open && (aw || bw)) ? q : 0.f;
-}
-
 template <int NWARP, int MINB, int UNROLL>
 __global__ void __launch_bounds__(NWARP * 32, MINB)
     stream_step_kernel(const GridDesc G, const ForcingDesc F, const StateBufs<float> S, const Thr<float> T,
@@ -239,45 +193,63 @@ __global__ void __launch_bounds__(NWARP * 32, MINB)
             const float umE = shdn(um1), umW = shup(um1);
             const float vnE = shdn(vn1), vnW = shup(vn1);
             const float vvW = shup(vv_1);
-            float rum_1 = 0.f, rvn_1 = 0.f;
-            {
-                const bool mA = (mb >> 2) & 1u, mB = (mb >> 1) & 1u, mLB = (mLb >> 1) & 1u;
-                const bool okx = col_cell && i > 0 && i < rows && mA && mB;
-                const bool oky = (unsigned)i < (unsigned)rows && gj > 0 && gj < cols && mLB && mB;
-                const bool wetx = okx && ((h2 >= gt_th) || (h1 >= gt_th));
-                const bool wety = oky && ((hL1 >= gt_th) || (h1 >= gt_th));
-                if (__any_sync(0xffffffffu, wetx || wety)) {
-                    FaceIn X;  // x-face (i, gj): a = (i-1, gj), b = (i, gj)
-                    X.ha = h2; X.hb = h1; X.za = z2; X.zb = z1;
-                    X.qc = um1; X.qf = um0; X.qb = um2; X.qe = umE; X.qw = umW;
-                    X.uf = 0.50f * (uu_0 + uu_1);
-                    X.ub = 0.50f * (uu_1 + uu_2);
-                    X.ve = 0.50f * (vvR_1 + vvR_2);
-                    X.vw = 0.50f * (vv_1 + vv_2);
-                    X.ufr = uu_1;
-                    X.vtr = 0.250f * (vv_1 + vvR_1 + vv_2 + vvR_2);
-                    X.rn = 0.5f * (n1 + n2);
-                    X.open = okx;
-                    X.along_on = true;
-                    X.across_on = gj != 0;  // cu:178-180
-                    FaceIn Y;  // y-face (i, gj): a = (i, gj-1), b = (i, gj)
-                    Y.ha = hL1; Y.hb = h1; Y.za = zL1; Y.zb = z1;
-                    Y.qc = vn1; Y.qf = vnE; Y.qb = vnW; Y.qe = vn0; Y.qw = vn2;
-                    Y.uf = 0.50f * (vvR_1 + vv_1);
-                    Y.ub = 0.50f * (vv_1 + vvW);
-                    Y.ve = 0.50f * (uu_0 + uuL_0);
-                    Y.vw = 0.50f * (uu_1 + uuL_1);
-                    Y.ufr = vv_1;
-                    Y.vtr = 0.250f * (uu_1 + uu_0 + uuL_1 + uuL_0);
-                    Y.rn = 0.5f * (n1 + nL1);
-                    Y.open = oky;
-                    Y.along_on = true;
-                    Y.across_on = i != 0;   // cu:289-291
-                    rum_1 = face_flux(X, T, g, dt2, dt2dx, dt2dy);
-                    rvn_1 = face_flux(Y, T, g, dt2, dt2dy, dt2dx);
+            float rum_1 = 0.f;
+            if (col_cell) {
+                if (i > 0 && i < rows) {
+                    const float ha = h2, hb = h1, za = z2, zb = z1;
+                    if (((mb >> 2) & (mb >> 1) & 1u) && ((ha >= gt_th) || (hb >= gt_th))) {
+                        if (!dry_bed<float>(T, g, ha, za, hb, zb, rum_1)) {
+                            const float hm = 0.50f * (hb + ha);
+                            const float u13 = g * hm * dt2dx * (hb + zb - ha - za);  // cu:166
+                            const float u11uur = 0.50f * (uu_0 + uu_1);
+                            const float u11uul = 0.50f * (uu_1 + uu_2);
+                            const float u11 = dt2dx * (upwind<float>(u11uur, um0, um1) - upwind_r<float>(u11uul, um2, um1));
+                            float u12 = 0.f;  // zero on column 0 (cu:178-180)
+                            if (gj != 0) {
+                                const float u12vvu = 0.50f * (vvR_1 + vvR_2);
+                                const float u12vvd = 0.50f * (vv_1 + vv_2);
+                                u12 = dt2dy * (upwind<float>(u12vvu, umE, um1) - upwind_r<float>(u12vvd, umW, um1));
+                            }
+                            const float rn = 0.5f * (n1 + n2);
+                            float ram = 0.f;
+                            if ((hm >= gt_th) && rn != 0.f) {  // cu:194-199
+                                const float vva = 0.250f * (vv_1 + vvR_1 + vv_2 + vvR_2);
+                                ram = g * rn * rn * sqrtf(uu_1 * uu_1 + vva * vva) / RT<float>::pow_(hm);
+                            }
+                            rum_1 = ((1.00f - dt2 * ram * 0.50f) * um1 + (-u11 - u12 - u13)) /
+                                    (1.00f + dt2 * ram * 0.50f);  // cu:203
+                        }
+                    }
+                } else if (i == rows && G.south_open) {  // free outfall (extension)
+                    if (((mb >> 2) & 1u) && h2 >= gt_th) rum_1 = 0.5440f * h2 * sqrtf(g * h2);
                 }
-                if (i == rows && G.south_open && col_cell && ((mb >> 2) & 1u) && h2 >= gt_th)
-                    rum_1 = 0.5440f * h2 * sqrtf(g * h2);  // free outfall (extension)
+            }
+            float rvn_1 = 0.f;
+            if ((unsigned)i < (unsigned)rows && gj > 0 && gj < cols) {
+                const float ha = hL1, hb = h1, za = zL1, zb = z1;
+                if (((mLb >> 1) & (mb >> 1) & 1u) && ((ha >= gt_th) || (hb >= gt_th))) {
+                    if (!dry_bed<float>(T, g, ha, za, hb, zb, rvn_1)) {
+                        const float hn = 0.50f * (hb + ha);
+                        const float v13 = g * hn * dt2dy * (hb + zb - ha - za);  // cu:283
+                        float v11 = 0.f;                                         // zero on row 0 (cu:289-291)
+                        if (i != 0) {
+                            const float v11uur = 0.50f * (uu_0 + uuL_0);
+                            const float v11uul = 0.50f * (uu_1 + uuL_1);
+                            v11 = dt2dx * (upwind<float>(v11uur, vn0, vn1) - upwind_r<float>(v11uul, vn2, vn1));
+                        }
+                        const float v12vvu = 0.50f * (vvR_1 + vv_1);
+                        const float v12vvd = 0.50f * (vv_1 + vvW);
+                        const float v12 = dt2dy * (upwind<float>(v12vvu, vnE, vn1) - upwind_r<float>(v12vvd, vnW, vn1));
+                        const float rn = 0.5f * (n1 + nL1);
+                        float ram = 0.f;
+                        if ((hn >= gt_th) && rn != 0.f) {  // cu:311-316
+                            const float uua = 0.250f * (uu_1 + uu_0 + uuL_1 + uuL_0);
+                            ram = g * rn * rn * sqrtf(uua * uua + vv_1 * vv_1) / RT<float>::pow_(hn);
+                        }
+                        rvn_1 = ((1.00f - dt2 * ram * 0.50f) * vn1 + (-v11 - v12 - v13)) /
+                                (1.00f + dt2 * ram * 0.50f);  // cu:320
+                    }
+                }
             }
 
             // ---- row r-2: provisional depth, forcing at t (cu:1278-1288) ----
