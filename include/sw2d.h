@@ -198,6 +198,38 @@ int sw2d_launch_count(sw2d_handle *h, int64_t *launches);
 const char *sw2d_last_error(const sw2d_handle *h);
 const char *sw2d_status_string(int32_t status);
 
+/* Largest grid sw2d_volume_noalloc accepts: 8192 x 8192 cells. */
+#define SW2D_NOALLOC_MAX_CELLS (8192LL * 8192LL)
+
+/* Volume of water [m^3] on the active cells of a depth field that the
+ * caller already holds on the device, for callers that cannot allocate
+ * device memory when they need the mass-balance check: a host model that
+ * captures its time loop into a CUDA graph in global capture mode (where
+ * cudaMalloc fails), or one whose memory pool has reserved the whole GPU.
+ * It allocates nothing: the partial sums live in a fixed 64 KiB array in
+ * the library's device image (one per GPU that loads the library, held
+ * until the process exits).  This entry point has no counterpart in the
+ * reference, which keeps no mass budget.
+ *
+ *   depth      device pointer, rows x cols float64 with a row pitch of
+ *              `pitch` elements (pitch >= cols)
+ *   mask       device pointer with the same layout, 1 = active cell, or
+ *              NULL when every cell counts
+ *   cell_area  dx * dy [m^2]
+ *   stream     cudaStream_t to run on (NULL = the legacy default stream);
+ *              the call returns after the result is on the host
+ *
+ * Returns SW2D_ERR_INVALID_ARG for null pointers, pitch < cols, a
+ * non-positive cell area, or rows * cols > SW2D_NOALLOC_MAX_CELLS.  The sum
+ * is deterministic (fixed chunks of 8192 cells, Kahan inside each chunk,
+ * chunks added in order).  The first call on a device looks up the scratch
+ * array's device address; make that first call before any stream capture.
+ * Every call reuses the same scratch array: calls that overlap on the GPU,
+ * from different streams or threads, race and must be serialised by the
+ * caller. */
+int sw2d_volume_noalloc(const double *depth, const uint8_t *mask, int32_t rows, int32_t cols, int32_t pitch,
+                        double cell_area, void *stream, double *volume_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -31,6 +31,7 @@ UNITS = {
     # the one device function here (the per-launch plan) must round like the
     # oracle: no contraction in device or host code
     "sw2d_api.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
+    "sw2d_noalloc.cu": ["--fmad=false"],
 }
 
 

@@ -77,6 +77,8 @@ _SIGS = {
     "sw2d_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "sw2d_last_error": (C.c_char_p, [C.c_void_p]),
     "sw2d_status_string": (C.c_char_p, [C.c_int32]),
+    "sw2d_volume_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_double,
+                                      C.c_void_p, C.POINTER(C.c_double)]),
 }
 
 
