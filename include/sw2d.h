@@ -198,6 +198,54 @@ int sw2d_launch_count(sw2d_handle *h, int64_t *launches);
 const char *sw2d_last_error(const sw2d_handle *h);
 const char *sw2d_status_string(int32_t status);
 
+/* ---------------------------------------------------------------------------
+ * Batched scenarios (extension; the reference runs one case at a time).
+ *
+ * A batch advances many FP32 scenarios of uneven size together: one
+ * persistent launch per iteration whose warps pull (scenario, column tile,
+ * row strip) units from a queue, each scenario with its own CFL time step,
+ * clock, forcing and end time, all state resident on the device.  Scenarios
+ * can be admitted (sw2d_batch_add) and retired (sw2d_batch_remove) between
+ * advances; memory is allocated and released stream-ordered.  A scenario
+ * advances bit for bit as it would alone in an FP32 handle.
+ * ------------------------------------------------------------------------- */
+typedef struct sw2d_batch sw2d_batch;
+
+typedef struct {
+    int32_t device;
+    int32_t max_scenarios; /* size of the scenario table */
+    int32_t max_units;     /* size of the work-unit table */
+    int32_t strip_h;       /* rows per warp, 0 = by scenario size */
+    int64_t max_bytes;     /* device budget for scenario data, 0 = none */
+    int32_t chunk;         /* launches per CUDA-graph replay (multiple of 3) */
+    int32_t reserved[3];
+} sw2d_batch_config;
+
+int sw2d_batch_config_init(sw2d_batch_config *cfg);
+/* Device bytes one scenario of this shape takes in a batch (admission). */
+int sw2d_batch_scenario_bytes(const sw2d_config *cfg, int32_t n_rain, int32_t with_raster, int64_t *bytes);
+int sw2d_batch_create(const sw2d_batch_config *cfg, sw2d_batch **out);
+int sw2d_batch_destroy(sw2d_batch *b);
+/* Admits a scenario (cfg: FP32, CFL rule) starting at t = 0 with depth,
+ * discharges 0, a uniform rain series and an end time; returns its id. */
+int sw2d_batch_add(sw2d_batch *b, const sw2d_config *cfg, const double *z, const double *manning,
+                   const double *depth, int32_t rain_kind, const double *rain, int32_t n_rain, double rain_dt,
+                   double t_end, int32_t *id);
+/* Enqueues `launches` iterations of every admitted scenario (finished ones
+ * idle).  With running != NULL, waits and returns how many still run. */
+int sw2d_batch_advance(sw2d_batch *b, int32_t launches, int32_t *running);
+/* Status of the admitted scenarios (waits for queued work): up to cap
+ * entries of id, running flag, simulated time and iterations; *n = count. */
+int sw2d_batch_poll(sw2d_batch *b, int32_t *ids, int32_t *running, double *t, int64_t *steps, int32_t cap,
+                    int32_t *n);
+int sw2d_batch_get_field(sw2d_batch *b, int32_t id, int32_t field, double *out);
+int sw2d_batch_get_budget(sw2d_batch *b, int32_t id, sw2d_budget *out);
+int sw2d_batch_remove(sw2d_batch *b, int32_t id);
+int sw2d_batch_bytes_in_use(sw2d_batch *b, int64_t *bytes);
+int sw2d_batch_get_stream(sw2d_batch *b, void **stream);
+int sw2d_batch_launch_count(sw2d_batch *b, int64_t *launches);
+const char *sw2d_batch_last_error(const sw2d_batch *b);
+
 /* Largest grid sw2d_volume_noalloc accepts: 8192 x 8192 cells. */
 #define SW2D_NOALLOC_MAX_CELLS (8192LL * 8192LL)
 

@@ -32,6 +32,8 @@ UNITS = {
     # oracle: no contraction in device or host code
     "sw2d_api.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "sw2d_noalloc.cu": ["--fmad=false"],
+    # same flags as step_f32.cu: a batched scenario advances bit for bit as alone
+    "sw2d_batch.cu": ["--use_fast_math"],
 }
 
 

@@ -26,13 +26,13 @@ cudaError_t launch_step(int th, int tw, int nblocks, const GridDesc &G, const Fo
 int stream_out_cols() { return kStreamOut; }
 
 // Builds of the streaming kernel the autotuner chooses from:
-// (warps per CTA, minimum resident CTAs per SM for the register budget, row-loop unrolling).
-#define SW2D_STREAM_VARIANTS(X) X(0, 4, 4, 1) X(1, 4, 1, 1) X(2, 4, 5, 1) X(3, 4, 6, 1) X(4, 4, 4, 2) X(5, 8, 2, 1)
+// (warps per CTA, minimum resident CTAs per SM, which sets the register budget).
+#define SW2D_STREAM_VARIANTS(X) X(0, 4, 4) X(1, 4, 1) X(2, 4, 5) X(3, 4, 6) X(4, 8, 2) X(5, 2, 8)
 
 int stream_variants() { return 6; }
 
 int stream_warps(int variant) {
-#define SW2D_W(id, nw, mb, un) \
+#define SW2D_W(id, nw, mb) \
     if (variant == id) return nw;
     SW2D_STREAM_VARIANTS(SW2D_W)
 #undef SW2D_W
@@ -40,9 +40,9 @@ int stream_warps(int variant) {
 }
 
 cudaError_t prepare_stream_step(int variant) {
-#define SW2D_P(id, nw, mb, un)                                                                               \
+#define SW2D_P(id, nw, mb)                                                                                   \
     if (variant == id)                                                                                      \
-        return cudaFuncSetAttribute(stream_step_kernel<nw, mb, un>, cudaFuncAttributePreferredSharedMemoryCarveout, \
+        return cudaFuncSetAttribute(stream_step_kernel<nw, mb>, cudaFuncAttributePreferredSharedMemoryCarveout, \
                                     (int)cudaSharedmemCarveoutMaxL1);
     SW2D_STREAM_VARIANTS(SW2D_P)
 #undef SW2D_P
@@ -57,9 +57,9 @@ cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_
     sh.strip_h = strip_h;
     sh.units = units;
     sh.pad = 0;
-#define SW2D_L(id, nw, mb, un)                                                                   \
+#define SW2D_L(id, nw, mb)                                                                       \
     if (variant == id) {                                                                         \
-        stream_step_kernel<nw, mb, un><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh); \
+        stream_step_kernel<nw, mb><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh);     \
         return cudaGetLastError();                                                               \
     }
     SW2D_STREAM_VARIANTS(SW2D_L)

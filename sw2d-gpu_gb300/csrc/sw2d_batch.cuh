@@ -1,0 +1,146 @@
+// sw2d_batch.cuh -- many scenarios of uneven size advanced by one persistent
+// FP32 launch per iteration.
+//
+// Each scenario keeps its own state, static fields, forcing, CFL time step
+// and clock (three rotating slots, as a single-scenario handle).  The work of
+// one launch is the list of (scenario, column tile, row strip) units of every
+// scenario in the batch; a fixed grid of CTAs pulls units from a queue head
+// (one atomic per unit), so scenarios of 64 x 64 and 2048 x 2048 cells share
+// the GPU without load imbalance.  A scenario's units take a ticket when they
+// finish; the last one finalises that scenario's clock slot (time, budgets,
+// CFL bound, the plan of its next iteration) -- no warp ever waits.
+//
+// The unit table, its length and the scenario descriptors live in device
+// memory, so the CUDA graph of launches stays valid while scenarios are
+// admitted and retired between replays.  A scenario whose plan says "stop"
+// (end time reached) costs one queue entry per unit and launch until it is
+// retired.
+#pragma once
+
+#include "sw2d_stream_unit.cuh"
+
+namespace sw2d {
+
+// Compact per-scenario status for the host, written by the finaliser.
+struct ScenarioStatus {
+    double t;
+    long long steps;
+    int running;     // the next iteration will run (end time not reached)
+    int nonfinite;
+    unsigned status;
+    int pad;
+};
+
+struct ScenarioDev {
+    GridDesc G;
+    ForcingDesc F;
+    Thr<float> T;
+    Control ctl;
+    float *h[2], *um[2], *vn[2];
+    const float *z, *nman;
+    const uint8_t *mask;
+    Clock *clk;                // three slots
+    ScenarioStatus *status;    // this scenario's entry of the batch status array
+    int tiles_w, strip_h, nunits, pad;
+};
+
+struct BatchHeader {
+    int n_units;               // length of the unit table
+    int pad;
+    unsigned int head[3];      // queue heads, one per launch parity
+    unsigned int pad2;
+};
+
+struct BatchDev {
+    ScenarioDev *scen;
+    const int2 *units;         // (scenario slot, unit index within the scenario)
+    BatchHeader *hdr;
+};
+
+__device__ inline void write_status(const Clock &c, ScenarioStatus *st) {
+    st->t = c.t;
+    st->steps = c.steps;
+    st->running = c.plan.run;
+    st->nonfinite = (int)c.nonfinite;
+    st->status = c.status;
+}
+
+template <int NWARP, int MINB>
+__global__ void __launch_bounds__(NWARP * 32, MINB) batch_step_kernel(const BatchDev B, const int slot) {
+    __shared__ int s_sr[NWARP][kStreamMaxSrc], s_sc[NWARP][kStreamMaxSrc];
+    __shared__ float s_q0[NWARP][kStreamMaxSrc], s_q1[NWARP][kStreamMaxSrc];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int slot_out = slot == 2 ? 0 : slot + 1;
+    const int slot_nx = slot == 0 ? 2 : slot - 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) B.hdr->head[slot_out] = 0u;  // queue of the next launch
+    const int n_units = B.hdr->n_units;
+    for (;;) {
+        unsigned u = 0;
+        if (lane == 0) u = atomicAdd(&B.hdr->head[slot], 1u);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= (unsigned)n_units) break;
+        const int2 ue = B.units[u];
+        const ScenarioDev &S = B.scen[ue.x];
+        const Clock &ci = S.clk[slot];
+        const int run = ci.plan.run;
+        if (run) {
+            StreamView V;
+            const int b = ci.buf;
+            V.rows = S.G.rows;
+            V.cols = S.G.cols;
+            V.pitch = S.G.pitch;
+            V.south_open = S.G.south_open;
+            V.Hin = S.h[b];
+            V.Uin = S.um[b];
+            V.Vin = S.vn[b];
+            V.Zin = S.z;
+            V.Nin = S.nman;
+            V.Min = S.mask;
+            V.Hout = S.h[1 - b];
+            V.Uout = S.um[1 - b];
+            V.Vout = S.vn[1 - b];
+            V.GS = S.G.sf;
+            V.T = S.T;
+            V.LS = ci.plan.f;
+            V.storm = S.F.rain_kind == RAIN_STORM;
+            V.on0 = ci.plan.storm_on0;
+            V.on1 = ci.plan.storm_on1;
+            V.n_src = S.G.n_src;
+            V.F = &S.F;
+            V.t0 = ci.plan.t0;
+            V.t1 = ci.plan.t1;
+            V.dx = S.G.dx;
+            V.dy = S.G.dy;
+            StreamAcc A;
+            A.rain = A.src = A.ev = A.out = A.clamp = A.cm = 0.f;
+            A.bad = A.too_many_sources = false;
+            const int ct = ue.y % S.tiles_w, rs = ue.y / S.tiles_w;
+            stream_unit(V, ct, rs, S.strip_h, lane, s_sr[wid], s_sc[wid], s_q0[wid], s_q1[wid], A);
+            warp_reduce_acc(A);
+            if (lane == 0) {
+                const double area = S.G.dx * S.G.dy, scale = ci.plan.d.dt2 * area;
+                double v[B_N];
+                v[B_RAIN] = (double)A.rain * scale;
+                v[B_SRC] = (double)A.src * scale;
+                v[B_EV] = (double)A.ev * scale;
+                v[B_OUT] = (double)A.out * ci.plan.d.dt2 * S.G.dy;
+                v[B_CLAMP] = (double)A.clamp * area;
+                accumulate_slot(S.clk[slot_out], ue.y % kBuckets, v, (double)A.cm, A.bad);
+                if (A.too_many_sources) atomicOr(&S.clk[slot_out].status, (unsigned)ST_TOO_MANY_LOCAL_SOURCES);
+            }
+        }
+        if (lane == 0) {
+            __threadfence();
+            const unsigned ticket = atomicAdd(&S.clk[slot_out].done_blocks, 1u);
+            if (ticket == (unsigned)S.nunits - 1u) {
+                __threadfence();
+                if (run) finalize_slot(ci, S.clk[slot_out], S.clk[slot_nx], ci.plan, S.ctl, S.G, S.F);
+                else carry_slot(ci, S.clk[slot_out], S.clk[slot_nx]);
+                write_status(S.clk[slot_out], S.status);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace sw2d

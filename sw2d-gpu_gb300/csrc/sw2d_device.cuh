@@ -336,15 +336,11 @@ __device__ inline void accumulate_slot(Clock &co, int bucket, const double v[B_N
     if (bad) atomicOr(&co.nonfinite, 1u);
 }
 
-// Called by one thread of every CTA after its accumulate_slot; the last CTA
-// of the launch finalises slot `co` (time, budgets, CFL bound, plan of the
-// next launch) and clears slot `cn` for the next launch.  No CTA waits.
-__device__ inline void finish_cta(const Clock &ci, Clock &co, Clock &cn, const Plan &pl, const Control &ctl,
-                                  const GridDesc &G, const ForcingDesc &F) {
-    __threadfence();
-    const unsigned int ticket = atomicAdd(&co.done_blocks, 1u);
-    if (ticket != gridDim.x * gridDim.y - 1) return;
-    __threadfence();
+// Finalises slot `co` once every contribution of the launch is in: sums the
+// buckets, folds the budgets, advances time, plans the next launch, and
+// clears slot `cn` for the launch after.  One thread.
+__device__ inline void finalize_slot(const Clock &ci, Clock &co, Clock &cn, const Plan &pl, const Control &ctl,
+                                     const GridDesc &G, const ForcingDesc &F) {
     volatile Clock *cov = &co;
     unsigned long long cm = 0ull;
     for (int b = 0; b < kBuckets; b++) {
@@ -369,6 +365,17 @@ __device__ inline void finish_cta(const Clock &ci, Clock &co, Clock &cn, const P
     co.status = cov->status | ci.status;
     co.plan = make_plan(t_new, cm, steps_new, ctl, G, F);
     clear_slot_accumulators(cn);
+}
+
+// Called by one thread of every CTA after its accumulate_slot; the last CTA
+// of the launch finalises the slot.  No CTA waits.
+__device__ inline void finish_cta(const Clock &ci, Clock &co, Clock &cn, const Plan &pl, const Control &ctl,
+                                  const GridDesc &G, const ForcingDesc &F) {
+    __threadfence();
+    const unsigned int ticket = atomicAdd(&co.done_blocks, 1u);
+    if (ticket != gridDim.x * gridDim.y - 1) return;
+    __threadfence();
+    finalize_slot(ci, co, cn, pl, ctl, G, F);
 }
 
 // ---------------------------------------------------------------------------

@@ -1,0 +1,323 @@
+// sw2d_stream_unit.cuh -- one warp's work in the FP32 streaming scheme: a
+// strip of rows of a 32-column window of one scenario (25 output columns).
+//
+// Shared by the single-scenario streaming kernel (sw2d_stream.cuh) and the
+// batched kernel (sw2d_batch.cuh); the arithmetic is that of step_kernel in
+// sw2d_device.cuh, organised as a 3-row register pipeline (see
+// sw2d_stream.cuh for the layout of the pipeline and the halo).
+#pragma once
+
+#include "sw2d_device.cuh"
+
+namespace sw2d {
+
+constexpr int kStreamHL = 4;                            // west halo lanes (3 + CFL ring)
+constexpr int kStreamHR = 3;                            // east halo lanes
+constexpr int kStreamOut = 32 - kStreamHL - kStreamHR;  // output columns per warp
+constexpr int kStreamMaxSrc = 16;                       // point sources per warp strip
+
+__device__ __forceinline__ float shup(float v) { return __shfl_up_sync(0xffffffffu, v, 1); }
+__device__ __forceinline__ float shdn(float v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+
+// Everything a warp reads to advance one strip of one scenario.
+struct StreamView {
+    int rows, cols, pitch, south_open;
+    const float *Hin, *Uin, *Vin, *Zin, *Nin;  // Nin == nullptr: scalar Manning n
+    const uint8_t *Min;
+    float *Hout, *Uout, *Vout;
+    GridScalars<float> GS;
+    Thr<float> T;
+    LaunchScalars<float> LS;
+    bool storm, on0, on1;
+    int n_src;                 // point sources of the scenario
+    const ForcingDesc *F;      // tables of the sources (only read when n_src > 0)
+    double t0, t1, dx, dy;     // for the source rates (FP64, once per warp)
+};
+
+// Per-warp results of a strip (per lane until reduced).
+struct StreamAcc {
+    float rain, src, ev, out, clamp, cm;
+    bool bad;
+    bool too_many_sources;
+};
+
+// Advances column tile `ct`, row strip `rs` (strip height strip_h) of the
+// scenario in V.  s_sr/s_sc/s_q0/s_q1 are this warp's slots for local point
+// sources (kStreamMaxSrc each).
+__device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, const int rs, const int strip_h,
+                                            const int lane, int *s_sr, int *s_sc, float *s_q0, float *s_q1,
+                                            StreamAcc &A) {
+    const int rows = V.rows, cols = V.cols, pitch = V.pitch;
+    const float dt2 = V.LS.dt2, dt2dx = V.LS.dt2dx, dt2dy = V.LS.dt2dy;
+    const float dx = V.GS.dx, dy = V.GS.dy, g = V.GS.g, manning = V.GS.manning, rdx = V.GS.rdx, rdy = V.GS.rdy;
+    const float pct_hi = V.GS.pct_hi, pct_lo = V.GS.pct_lo;
+    const Thr<float> T = V.T;
+    const float gt_th = T.gt_th, ge_th = T.ge_th, gt_ev = T.gt_evmin;
+    const bool raster = V.Nin != nullptr;
+    const float *__restrict__ Hin = V.Hin;
+    const float *__restrict__ Uin = V.Uin;
+    const float *__restrict__ Vin = V.Vin;
+    const float *__restrict__ Zin = V.Zin;
+    const float *__restrict__ Nin = V.Nin;
+    const uint8_t *__restrict__ Min = V.Min;
+    float *__restrict__ Hout = V.Hout;
+    float *__restrict__ Uout = V.Uout;
+    float *__restrict__ Vout = V.Vout;
+
+    const int gj0 = ct * kStreamOut - kStreamHL;
+    const int gj = gj0 + lane;
+    const int R0 = rs * strip_h;
+    const int R1 = min(R0 + strip_h, rows);
+    const bool out_col = lane >= kStreamHL && lane < kStreamHL + kStreamOut && gj < cols;
+    const bool col_cell = (unsigned)gj < (unsigned)cols;
+    const bool col_vn = (unsigned)gj <= (unsigned)cols;
+
+    // point sources inside this warp's window, in list order (the later one
+    // wins on a shared cell, as the reference's assignment, cu:545)
+    int nsrc = 0;
+    if (V.n_src > 0) {
+        const double area = V.dx * V.dy;
+        for (int base = 0; base < V.n_src; base += 32) {
+            const int s = base + lane;
+            bool in = false;
+            int sr = 0, sc = 0;
+            if (s < V.n_src) {
+                const int cell = V.F->src_cell[s];
+                sr = cell / cols;
+                sc = cell - sr * cols;
+                in = sr >= R0 - 4 && sr < R1 + 3 && sc >= gj0 && sc < gj0 + 32;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, in);
+            if (in) {
+                const int off = nsrc + __popc(bal & ((1u << lane) - 1u));
+                if (off < kStreamMaxSrc) {
+                    s_sr[off] = sr;
+                    s_sc[off] = sc;
+                    s_q0[off] = (float)source_rate(*V.F, V.n_src, s, V.t0, area);
+                    s_q1[off] = (float)source_rate(*V.F, V.n_src, s, V.t1, area);
+                } else {
+                    A.too_many_sources = true;
+                }
+            }
+            nsrc += __popc(bal);
+        }
+        __syncwarp();
+        nsrc = min(nsrc, kStreamMaxSrc);
+    }
+    auto source_at = [&](int row, bool second) -> float {
+        float q = 0.f;
+        for (int e = 0; e < nsrc; e++)
+            if (s_sr[e] == row && s_sc[e] == gj) q = second ? s_q1[e] : s_q0[e];
+        return q;
+    };
+    auto storm_rate = [&](int row, bool on, float sx, float sy) -> float {
+        if (!on) return 0.f;
+        const float x = ((float)gj + 0.5f) * dx - sx;
+        const float y = ((float)row + 0.5f) * dy - sy;
+        return V.GS.storm_amp * __expf(-(x * x + y * y) / V.GS.storm_2s2);
+    };
+
+    // row loads (zero outside the domain: inactive cells, walls)
+    float p_h, p_z, p_n, p_um, p_vn;
+    unsigned p_m;
+    auto load_row = [&](int r) {
+        const bool rc = (unsigned)r < (unsigned)rows;
+        const size_t gp = (size_t)r * pitch + gj;
+        const bool cell = rc && col_cell;
+        p_h = cell ? Hin[gp] : 0.f;
+        p_z = cell ? Zin[gp] : 0.f;
+        p_n = (cell && raster) ? Nin[gp] : manning;
+        p_m = cell ? (unsigned)Min[gp] : 0u;
+        p_um = ((unsigned)r <= (unsigned)rows && col_cell) ? Uin[gp] : 0.f;
+        p_vn = (rc && col_vn) ? Vin[gp] : 0.f;
+    };
+
+    // register rings: suffix = rows back from the row being read (r)
+    float h1 = 0.f, h2 = 0.f, h3 = 0.f, hL1 = 0.f;
+    float z1 = 0.f, z2 = 0.f, zL1 = 0.f;
+    float n1 = manning, n2 = manning, nL1 = manning;
+    float um1 = 0.f, um2 = 0.f, vn1 = 0.f, vn2 = 0.f;
+    float uu_1 = 0.f, uu_2 = 0.f, uuL_1 = 0.f;
+    float vv_1 = 0.f, vv_2 = 0.f, vvR_2 = 0.f;
+    float rum_2 = 0.f, rum_3 = 0.f, rvn_2 = 0.f, rvn_3 = 0.f;
+    float hs_3 = 0.f, hs_4 = 0.f, hw_4 = 0.f;
+    unsigned mb = 0u, mLb = 0u;  // bit k: active mask of row r-k (own / west column)
+
+    const int r_first = R0 - 4, r_last = R1 + 3;
+    load_row(r_first);
+#pragma unroll 1
+    for (int r = r_first; r < r_last; r++) {
+        const float h0 = p_h, z0 = p_z, n0 = p_n, um0 = p_um, vn0 = p_vn;
+        mb = (mb << 1) | p_m;
+        const unsigned mL0 = __shfl_up_sync(0xffffffffu, p_m, 1);
+        mLb = (mLb << 1) | mL0;
+        if (r + 1 < r_last) load_row(r + 1);  // prefetch
+
+        const float hL0 = shup(h0), zL0 = shup(z0);
+        const float nL0 = raster ? shup(n0) : manning;
+        // ---- row r: face velocities (cu:363-453) ----
+        const float hnf = (gj == cols) ? hL0 : ((gj == 0) ? h0 : 0.50f * (h0 + hL0));
+        const float vv_0 = (hnf >= ge_th) ? vn0 / hnf : 0.0f;
+        const float hmf = (r == rows) ? h1 : ((r == 0) ? h0 : 0.50f * (h0 + h1));
+        const float uu_0 = (hmf >= ge_th) ? um0 / hmf : 0.0f;
+        const float uuL_0 = shup(uu_0);
+        const float vvR_1 = shdn(vv_1);
+
+        // ---- row r-1: new face discharges (cu:98-354) ----
+        const int i = r - 1;
+        const float umE = shdn(um1), umW = shup(um1);
+        const float vnE = shdn(vn1), vnW = shup(vn1);
+        const float vvW = shup(vv_1);
+        float rum_1 = 0.f;
+        if (col_cell) {
+            if (i > 0 && i < rows) {
+                const float ha = h2, hb = h1, za = z2, zb = z1;
+                if (((mb >> 2) & (mb >> 1) & 1u) && ((ha >= gt_th) || (hb >= gt_th))) {
+                    if (!dry_bed<float>(T, g, ha, za, hb, zb, rum_1)) {
+                        const float hm = 0.50f * (hb + ha);
+                        const float u13 = g * hm * dt2dx * (hb + zb - ha - za);  // cu:166
+                        const float u11uur = 0.50f * (uu_0 + uu_1);
+                        const float u11uul = 0.50f * (uu_1 + uu_2);
+                        const float u11 = dt2dx * (upwind<float>(u11uur, um0, um1) - upwind_r<float>(u11uul, um2, um1));
+                        float u12 = 0.f;  // zero on column 0 (cu:178-180)
+                        if (gj != 0) {
+                            const float u12vvu = 0.50f * (vvR_1 + vvR_2);
+                            const float u12vvd = 0.50f * (vv_1 + vv_2);
+                            u12 = dt2dy * (upwind<float>(u12vvu, umE, um1) - upwind_r<float>(u12vvd, umW, um1));
+                        }
+                        const float rn = 0.5f * (n1 + n2);
+                        float ram = 0.f;
+                        if ((hm >= gt_th) && rn != 0.f) {  // cu:194-199
+                            const float vva = 0.250f * (vv_1 + vvR_1 + vv_2 + vvR_2);
+                            ram = g * rn * rn * sqrtf(uu_1 * uu_1 + vva * vva) / RT<float>::pow_(hm);
+                        }
+                        rum_1 = ((1.00f - dt2 * ram * 0.50f) * um1 + (-u11 - u12 - u13)) /
+                                (1.00f + dt2 * ram * 0.50f);  // cu:203
+                    }
+                }
+            } else if (i == rows && V.south_open) {  // free outfall (extension)
+                if (((mb >> 2) & 1u) && h2 >= gt_th) rum_1 = 0.5440f * h2 * sqrtf(g * h2);
+            }
+        }
+        float rvn_1 = 0.f;
+        if ((unsigned)i < (unsigned)rows && gj > 0 && gj < cols) {
+            const float ha = hL1, hb = h1, za = zL1, zb = z1;
+            if (((mLb >> 1) & (mb >> 1) & 1u) && ((ha >= gt_th) || (hb >= gt_th))) {
+                if (!dry_bed<float>(T, g, ha, za, hb, zb, rvn_1)) {
+                    const float hn = 0.50f * (hb + ha);
+                    const float v13 = g * hn * dt2dy * (hb + zb - ha - za);  // cu:283
+                    float v11 = 0.f;                                         // zero on row 0 (cu:289-291)
+                    if (i != 0) {
+                        const float v11uur = 0.50f * (uu_0 + uuL_0);
+                        const float v11uul = 0.50f * (uu_1 + uuL_1);
+                        v11 = dt2dx * (upwind<float>(v11uur, vn0, vn1) - upwind_r<float>(v11uul, vn2, vn1));
+                    }
+                    const float v12vvu = 0.50f * (vvR_1 + vv_1);
+                    const float v12vvd = 0.50f * (vv_1 + vvW);
+                    const float v12 = dt2dy * (upwind<float>(v12vvu, vnE, vn1) - upwind_r<float>(v12vvd, vnW, vn1));
+                    const float rn = 0.5f * (n1 + nL1);
+                    float ram = 0.f;
+                    if ((hn >= gt_th) && rn != 0.f) {  // cu:311-316
+                        const float uua = 0.250f * (uu_1 + uu_0 + uuL_1 + uuL_0);
+                        ram = g * rn * rn * sqrtf(uua * uua + vv_1 * vv_1) / RT<float>::pow_(hn);
+                    }
+                    rvn_1 = ((1.00f - dt2 * ram * 0.50f) * vn1 + (-v11 - v12 - v13)) /
+                            (1.00f + dt2 * ram * 0.50f);  // cu:320
+                }
+            }
+        }
+
+        // ---- row r-2: provisional depth, forcing at t (cu:1278-1288) ----
+        const float rvnE_2 = shdn(rvn_2);
+        float hs_2 = 0.f;
+        if ((mb >> 2) & 1u) {
+            const float ho = h2;
+            const bool hi = ho >= gt_ev;
+            const float pct = hi ? pct_hi : pct_lo;
+            const float evapo = hi ? V.LS.ev0 : 0.f;
+            const float ql = nsrc ? source_at(r - 2, false) : 0.f;
+            const float rr = V.storm ? storm_rate(r - 2, V.on0, V.LS.sx0, V.LS.sy0) : V.LS.rr0;
+            hs_2 = fmaxf(ho - dt2 * ((rum_1 - rum_2) * rdx + (rvnE_2 - rvn_2) * rdy - ql - rr * pct + evapo), 0.f);
+        }
+
+        // ---- row r-3: dry-cell fix (cu:695-725) and final depth ----
+        const float hsW_3 = shup(hs_3);
+        const bool m3 = (mb >> 3) & 1u, m4 = (mb >> 4) & 1u, m2 = (mb >> 2) & 1u, mL3 = (mLb >> 3) & 1u;
+        float un = rum_3;  // x-face north of the row-(r-3) cell
+        if ((un > 0.f && m4 && !(hs_4 >= ge_th)) || (un < 0.f && m3 && !(hs_3 >= ge_th))) un = 0.f;
+        float us = rum_2;  // x-face south of it
+        if ((us > 0.f && m3 && !(hs_3 >= ge_th)) || (us < 0.f && m2 && !(hs_2 >= ge_th))) us = 0.f;
+        float vw = rvn_3;  // y-face west of it
+        if ((vw > 0.f && mL3 && !(hsW_3 >= ge_th)) || (vw < 0.f && m3 && !(hs_3 >= ge_th))) vw = 0.f;
+        const float ve = shdn(vw);
+        const int f = r - 3;
+        float hw_3 = 0.f, hraw = 0.f, rr1 = 0.f, pct1 = 0.f, ev1 = 0.f, ql1 = 0.f;
+        if (m3) {
+            const float ho = h3;
+            const bool hi = ho >= gt_ev;
+            pct1 = hi ? pct_hi : pct_lo;
+            ev1 = hi ? V.LS.ev1 : 0.f;
+            ql1 = nsrc ? source_at(f, true) : 0.f;
+            rr1 = V.storm ? storm_rate(f, V.on1, V.LS.sx1, V.LS.sy1) : V.LS.rr1;
+            hraw = ho - dt2 * ((us - un) * rdx + (ve - vw) * rdy - ql1 - rr1 * pct1 + ev1);
+            hw_3 = fmaxf(hraw, 0.f);
+        }
+        const float hwW = shup(hw_3);
+        if (out_col && f >= R0 && f < R1) {
+            const size_t gp = (size_t)f * pitch + gj;
+            Hout[gp] = hw_3;
+            Uout[gp] = un;
+            Vout[gp] = vw;
+            if (f == rows - 1) {
+                Uout[gp + pitch] = us;
+                A.out += us;
+            }
+            if (m3) {
+                A.rain += rr1 * pct1;
+                A.src += ql1;
+                A.ev += ev1;
+                if (hraw < 0.f) A.clamp -= hraw;
+                // CFL bound of the new state on the owned faces (extension)
+                if (f > 0 && m4) {
+                    const float hm = 0.50f * (hw_3 + hw_4);
+                    if (hm >= ge_th) A.cm = fmaxf(A.cm, fabsf(un / hm) + sqrtf(g * hm));
+                }
+                if (f == rows - 1 && V.south_open && hw_3 >= ge_th)
+                    A.cm = fmaxf(A.cm, fabsf(us / hw_3) + sqrtf(g * hw_3));
+                if (gj > 0 && mL3) {
+                    const float hn = 0.50f * (hw_3 + hwW);
+                    if (hn >= ge_th) A.cm = fmaxf(A.cm, fabsf(vw / hn) + sqrtf(g * hn));
+                }
+            }
+            if (!isfinite(hw_3) || !isfinite(un) || !isfinite(vw)) A.bad = true;
+        }
+
+        // ---- advance the rings ----
+        h3 = h2; h2 = h1; h1 = h0; hL1 = hL0;
+        z2 = z1; z1 = z0; zL1 = zL0;
+        n2 = n1; n1 = n0; nL1 = nL0;
+        um2 = um1; um1 = um0; vn2 = vn1; vn1 = vn0;
+        uu_2 = uu_1; uu_1 = uu_0; uuL_1 = uuL_0;
+        vv_2 = vv_1; vv_1 = vv_0; vvR_2 = vvR_1;
+        rum_3 = rum_2; rum_2 = rum_1; rvn_3 = rvn_2; rvn_2 = rvn_1;
+        hs_4 = hs_3; hs_3 = hs_2;
+        hw_4 = hw_3;
+    }
+}
+
+// Warp reduction of a StreamAcc: sums / max / any into lane 0's return.
+__device__ __forceinline__ void warp_reduce_acc(StreamAcc &A) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        A.rain += __shfl_xor_sync(0xffffffffu, A.rain, o);
+        A.src += __shfl_xor_sync(0xffffffffu, A.src, o);
+        A.ev += __shfl_xor_sync(0xffffffffu, A.ev, o);
+        A.out += __shfl_xor_sync(0xffffffffu, A.out, o);
+        A.clamp += __shfl_xor_sync(0xffffffffu, A.clamp, o);
+        A.cm = fmaxf(A.cm, __shfl_xor_sync(0xffffffffu, A.cm, o));
+    }
+    A.bad = __any_sync(0xffffffffu, A.bad);
+    A.too_many_sources = __any_sync(0xffffffffu, A.too_many_sources);
+}
+
+}  // namespace sw2d

@@ -48,6 +48,13 @@ class Budget(C.Structure):
     ]
 
 
+class BatchConfig(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32), ("max_scenarios", C.c_int32), ("max_units", C.c_int32), ("strip_h", C.c_int32),
+        ("max_bytes", C.c_int64), ("chunk", C.c_int32), ("reserved", C.c_int32 * 3),
+    ]
+
+
 class SW2DError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__(f"{msg} (status {status})")
@@ -79,6 +86,22 @@ _SIGS = {
     "sw2d_status_string": (C.c_char_p, [C.c_int32]),
     "sw2d_volume_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_double,
                                       C.c_void_p, C.POINTER(C.c_double)]),
+    "sw2d_batch_config_init": (C.c_int, [C.POINTER(BatchConfig)]),
+    "sw2d_batch_scenario_bytes": (C.c_int, [C.POINTER(Config), C.c_int32, C.c_int32, C.POINTER(C.c_int64)]),
+    "sw2d_batch_create": (C.c_int, [C.POINTER(BatchConfig), C.POINTER(C.c_void_p)]),
+    "sw2d_batch_destroy": (C.c_int, [C.c_void_p]),
+    "sw2d_batch_add": (C.c_int, [C.c_void_p, C.POINTER(Config), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                 C.c_void_p, C.c_int32, C.c_double, C.c_double, C.POINTER(C.c_int32)]),
+    "sw2d_batch_advance": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
+    "sw2d_batch_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                  C.POINTER(C.c_int32)]),
+    "sw2d_batch_get_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+    "sw2d_batch_get_budget": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(Budget)]),
+    "sw2d_batch_remove": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sw2d_batch_bytes_in_use": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "sw2d_batch_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "sw2d_batch_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "sw2d_batch_last_error": (C.c_char_p, [C.c_void_p]),
 }
 
 
@@ -245,3 +268,116 @@ class Solver:
         out = np.empty(cells.size, dtype=np.float64)
         self._check(load().sw2d_probe(self._h, _p(cells), cells.size, _p(out)), "sw2d_probe")
         return out
+
+
+def batch_config(**kw) -> BatchConfig:
+    c = BatchConfig()
+    load().sw2d_batch_config_init(C.byref(c))
+    for k, v in kw.items():
+        if not hasattr(c, k):
+            raise AttributeError(f"sw2d_batch_config has no field {k}")
+        setattr(c, k, v)
+    return c
+
+
+def batch_scenario_bytes(cfg: Config, n_rain=0, with_raster=True) -> int:
+    b = C.c_int64()
+    st = load().sw2d_batch_scenario_bytes(C.byref(cfg), int(n_rain), int(bool(with_raster)), C.byref(b))
+    if st != OK:
+        raise SW2DError(st, "sw2d_batch_scenario_bytes")
+    return int(b.value)
+
+
+class Batch:
+    """Many FP32 scenarios advanced together on one GPU (C-ABI sw2d_batch_*)."""
+
+    def __init__(self, cfg: BatchConfig | None = None, **kw):
+        L = load()
+        self.cfg = cfg if cfg is not None else batch_config(**kw)
+        h = C.c_void_p()
+        st = L.sw2d_batch_create(C.byref(self.cfg), C.byref(h))
+        if st != OK:
+            raise SW2DError(st, "sw2d_batch_create failed")
+        self._h = h
+        self.shapes = {}
+
+    def _check(self, st, what):
+        if st != OK:
+            raise SW2DError(st, f"{what}: {load().sw2d_batch_last_error(self._h).decode()}")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().sw2d_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def add(self, cfg: Config, z, depth, manning=None, rain_kind=RAIN_NONE, rain=None, rain_dt=1.0, t_end=1e300):
+        r, c = cfg.rows, cfg.cols
+        z = _f64(z, (r, c))
+        d = _f64(depth, (r, c))
+        n = _f64(manning, (r, c)) if manning is not None else None
+        rs = _f64(np.atleast_1d(rain)) if rain is not None else None
+        sid = C.c_int32()
+        self._check(load().sw2d_batch_add(self._h, C.byref(cfg), _p(z), _p(n), _p(d), int(rain_kind), _p(rs),
+                                          0 if rs is None else rs.size, float(rain_dt), float(t_end), C.byref(sid)),
+                    "sw2d_batch_add")
+        self.shapes[sid.value] = (r, c)
+        return sid.value
+
+    def advance(self, launches, wait=True):
+        run = C.c_int32()
+        self._check(load().sw2d_batch_advance(self._h, int(launches), C.byref(run) if wait else None),
+                    "sw2d_batch_advance")
+        return run.value if wait else None
+
+    def poll(self):
+        cap = max(len(self.shapes), 1)
+        ids = np.zeros(cap, np.int32); run = np.zeros(cap, np.int32); t = np.zeros(cap); steps = np.zeros(cap, np.int64)
+        n = C.c_int32()
+        self._check(load().sw2d_batch_poll(self._h, _p(ids), _p(run), _p(t), _p(steps), cap, C.byref(n)),
+                    "sw2d_batch_poll")
+        k = n.value
+        return {int(i): {"running": bool(rr), "t": float(tt), "steps": int(ss)}
+                for i, rr, tt, ss in zip(ids[:k], run[:k], t[:k], steps[:k])}
+
+    def field(self, sid, which=FIELD_DEPTH):
+        r, c = self.shapes[sid]
+        shape = {FIELD_UM: (r + 1, c), FIELD_VN: (r, c + 1)}.get(which, (r, c))
+        out = np.empty(shape)
+        self._check(load().sw2d_batch_get_field(self._h, int(sid), int(which), _p(out)), "sw2d_batch_get_field")
+        return out
+
+    def budget(self, sid):
+        b = Budget()
+        self._check(load().sw2d_batch_get_budget(self._h, int(sid), C.byref(b)), "sw2d_batch_get_budget")
+        return {k: getattr(b, k) for k, _ in Budget._fields_ if k != "reserved"}
+
+    def remove(self, sid):
+        self._check(load().sw2d_batch_remove(self._h, int(sid)), "sw2d_batch_remove")
+        self.shapes.pop(sid, None)
+
+    def bytes_in_use(self):
+        v = C.c_int64()
+        self._check(load().sw2d_batch_bytes_in_use(self._h, C.byref(v)), "sw2d_batch_bytes_in_use")
+        return int(v.value)
+
+    def stream(self):
+        s = C.c_void_p()
+        self._check(load().sw2d_batch_get_stream(self._h, C.byref(s)), "sw2d_batch_get_stream")
+        return int(s.value or 0)
+
+    def launch_count(self):
+        v = C.c_int64()
+        self._check(load().sw2d_batch_launch_count(self._h, C.byref(v)), "sw2d_batch_launch_count")
+        return int(v.value)
