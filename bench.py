@@ -250,6 +250,10 @@ def run_ours(args):
     d2h = SIZE * SIZE * 8 + k_e2e * (1024 * 8 + 200)
     assert np.isfinite(out_h).all()
 
+    # ---- batched ensemble and served stream (extra keys) --------------------
+    batched = run_batched(sw2d, dev, args) if args.batched else None
+    served = run_served(sw2d, dev, args) if args.served else None
+
     # ---- CPU baseline: the oracle on a bounded sample ------------------------
     cpu = cpu_sample(s, spun, budget_s=args.cpu_seconds) if rank == 0 else None
 
@@ -266,7 +270,7 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": (tpc * active if tpc is not None else None),
-                         "bytes_alg_per_cell_update": B_ALG_F32, "kernel": "step_kernel<float,16,32,256>",
+                         "bytes_alg_per_cell_update": B_ALG_F32, "kernel": "stream_step_kernel<4,4>",
                          "launch_s": per_launch},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / k_e2e,
@@ -276,10 +280,102 @@ def run_ours(args):
             "wall_s_timed": wall,
             "fp64_plain": {"value": v64, "unit": "cell-updates/s", "speedup_f32_over_f64": value / ws / v64},
             "volume_rel_error": vol_err,
+            "batched": batched,
+            "served": served,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+_BANK = None
+
+
+def terrain_bank():
+    global _BANK
+    if _BANK is None:
+        from sw2d import scenarios as S
+        _BANK = S.TerrainBank(size=SIZE, dx=DX, seed=SEED + 7)
+    return _BANK
+
+
+def scen_cfg(sw2d, side, precision=None, device=0):
+    return sw2d.default_config(rows=side, cols=side, dx=DX, dy=DX,
+                               precision=sw2d.PREC_F32 if precision is None else precision,
+                               dt_mode=sw2d.DT_CFL, dt=DT_MAX, cfl=0.5, south_open=1, device=device)
+
+
+def run_batched(sw2d, dev, args):
+    """The batched-ensemble configuration: 256 scenarios, sides uniform over
+    {128, 256, 512, 1024}, triangular hyetographs, Manning scaling, horizon =
+    rain duration + 1800 s; all advanced together until the last one ends.
+    The serial FP64 plain path is timed on one scenario per size class and
+    extrapolated with the ensemble's own iteration counts."""
+    import torch
+    from sw2d import scenarios as S
+    ens = S.ensemble(terrain_bank(), count=args.batch_count, seed=SEED + 11)
+    t0 = time.perf_counter()
+    b = sw2d.Batch(device=dev, chunk=24, max_scenarios=len(ens) + 8)
+    ids = [b.add(scen_cfg(sw2d, e["side"], device=dev), e["z"], e["h0"], manning=e["n"],
+                 rain_kind=sw2d.RAIN_LINEAR, rain=e["rain"], rain_dt=e["rain_dt"], t_end=e["t_end"]) for e in ens]
+    t_admit = time.perf_counter() - t0
+    st = torch.cuda.ExternalStream(b.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    launches0 = b.launch_count()
+    running = len(ids)
+    while running:
+        running = b.advance(48)
+    e1.record(st)
+    e1.synchronize()
+    gpu_s = e0.elapsed_time(e1) / 1e3
+    wall = time.perf_counter() - t0
+    status = b.poll()
+    cu = sum(e["side"] * e["side"] * status[i]["steps"] for e, i in zip(ens, ids))
+    launches = b.launch_count() - launches0
+    b.close()
+    # serial FP64 plain path, per size class
+    rate64 = {}
+    for side in sorted({e["side"] for e in ens}):
+        e = next(x for x in ens if x["side"] == side)
+        g = sw2d.Solver(scen_cfg(sw2d, side, precision=sw2d.PREC_F64, device=dev))
+        g.set_static(e["z"], e["n"])
+        g.set_state(np.full((side, side), 0.005))
+        g.set_rain(sw2d.RAIN_LINEAR, e["rain"], e["rain_dt"])
+        g.advance(6)
+        g.synchronize()
+        tt = time.perf_counter()
+        n = g.advance(max(6, int(2e8 / (side * side))))
+        g.synchronize()
+        rate64[side] = side * side * n / (time.perf_counter() - tt)
+        g.close()
+    serial64_s = sum(e["side"] * e["side"] * status[i]["steps"] / rate64[e["side"]] for e, i in zip(ens, ids))
+    return {"scenarios": len(ens), "cells": int(sum(e["side"] ** 2 for e in ens)), "cell_updates": int(cu),
+            "gpu_s": gpu_s, "wall_s_incl_admission": wall, "admission_s": t_admit, "launches": int(launches),
+            "cell_updates_per_s": cu / gpu_s, "scenarios_per_hour": len(ens) / wall * 3600.0,
+            "serial_fp64_plain_s_est": serial64_s, "fp64_plain_rate_by_side": {str(k): v for k, v in rate64.items()},
+            "scenario_throughput_vs_serial_fp64": serial64_s / wall,
+            "horizon": "rain duration + 1800 s"}
+
+
+def run_served(sw2d, dev, args):
+    """The served-stream configuration at one arrival rate: log-uniform
+    sides 64-2048 (multiples of 32), horizons U[600, 7200] s, Poisson
+    arrivals; continuous batching with admission by device footprint."""
+    from sw2d import scenarios as S
+    from sw2d import serve
+    specs = S.request_stream(terrain_bank(), rate=args.serve_rate, count=args.serve_count, seed=SEED + 13)
+    reqs = [serve.Request(rid=k, arrival=sp["arrival"], cfg=scen_cfg(sw2d, sp["side"], device=dev), z=sp["z"],
+                          depth=sp["h0"], manning=sp["n"], rain_kind=sw2d.RAIN_LINEAR, rain=sp["rain"],
+                          rain_dt=sp["rain_dt"], t_end=sp["t_end"]) for k, sp in enumerate(specs)]
+    budget = int(args.serve_gb * 2 ** 30)
+    srv = serve.Server(lambda: sw2d.Batch(device=dev, chunk=24, max_scenarios=len(reqs) + 8, max_bytes=budget),
+                       bytes_of=lambda r: sw2d.batch_scenario_bytes(r.cfg, 3, True), max_bytes=budget,
+                       launches_per_tick=24)
+    st = srv.run(reqs, timeout=600.0)
+    srv.batch.close()
+    st.update({"rate_per_s": args.serve_rate, "memory_budget_gb": args.serve_gb})
+    return st
 
 
 def cpu_sample(s, spun, budget_s=12.0):
@@ -340,6 +436,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--batched", type=int, default=1, help="run the batched-ensemble leg")
+    ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--served", type=int, default=1, help="run the served-stream leg")
+    ap.add_argument("--serve-rate", type=float, default=10.0)
+    ap.add_argument("--serve-count", type=int, default=100)
+    ap.add_argument("--serve-gb", type=float, default=40.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -118,3 +118,62 @@ def triangular_hyetograph(peak_mm_h, duration_s):
     """Knots (mm/h) of a triangular hyetograph for RAIN_LINEAR: 0 at t=0,
     peak at duration/2, 0 at duration; knot spacing duration/2."""
     return np.array([0.0, float(peak_mm_h), 0.0]), duration_s / 2.0
+
+
+class TerrainBank:
+    """Scenario terrains cut from one seeded master catchment.
+
+    Generating a fresh fractal DEM per scenario costs seconds at 1024^2; an
+    ensemble or a request stream instead takes seeded random windows of one
+    master catchment (same slope, noise statistics and Voronoi roughness
+    classes), so each scenario still has its own terrain."""
+
+    def __init__(self, size=2048, dx=5.0, seed=0):
+        self.master = catchment(size, dx=dx, seed=seed)
+        self.size, self.dx = size, dx
+
+    def crop(self, side, rng, manning_scale=1.0):
+        side = min(int(side), self.size)
+        i0 = int(rng.integers(0, self.size - side + 1))
+        j0 = int(rng.integers(0, self.size - side + 1))
+        z = np.ascontiguousarray(self.master["z"][i0:i0 + side, j0:j0 + side])
+        n = np.ascontiguousarray(self.master["n"][i0:i0 + side, j0:j0 + side]) * manning_scale
+        return {"z": z, "h0": np.zeros((side, side)), "n": n, "dx": self.dx}
+
+
+def ensemble(bank, count=256, sides=(128, 256, 512, 1024), seed=1, tail=1800.0):
+    """The batched-ensemble configuration: sides uniform over `sides`, each
+    scenario with a triangular hyetograph (peak U[20,120] mm/h, duration
+    U[900,3600] s) and a Manning scaling U[0.8,1.2]; horizon = duration +
+    `tail` seconds (the configuration does not give one)."""
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    out = []
+    for _ in range(count):
+        side = int(rng.choice(sides))
+        peak = float(rng.uniform(20.0, 120.0))
+        dur = float(rng.uniform(900.0, 3600.0))
+        s = bank.crop(side, rng, manning_scale=float(rng.uniform(0.8, 1.2)))
+        knots, kdt = triangular_hyetograph(peak, dur)
+        s.update(rain=knots, rain_dt=kdt, t_end=dur + tail, side=side)
+        out.append(s)
+    return out
+
+
+def request_stream(bank, rate, count, seed=2, side_min=64, side_max=2048, horizon=(600.0, 7200.0)):
+    """The served-stream configuration: Poisson arrivals at `rate`/s, grid
+    side log-uniform over [side_min, side_max] rounded to a multiple of 32,
+    simulated horizon uniform over `horizon`, triangular rain as above."""
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    t = np.cumsum(rng.exponential(1.0 / rate, size=count))
+    out = []
+    for k in range(count):
+        side = float(np.exp(rng.uniform(np.log(side_min), np.log(side_max))))
+        side = int(max(32, min(side_max, 32 * round(side / 32))))
+        h_end = float(rng.uniform(*horizon))
+        peak = float(rng.uniform(20.0, 120.0))
+        dur = float(rng.uniform(900.0, 3600.0))
+        s = bank.crop(side, rng, manning_scale=float(rng.uniform(0.8, 1.2)))
+        knots, kdt = triangular_hyetograph(peak, dur)
+        s.update(rain=knots, rain_dt=kdt, t_end=h_end, side=side, arrival=float(t[k]))
+        out.append(s)
+    return out

@@ -1,0 +1,158 @@
+"""Continuous batching of flood scenarios on one GPU.
+
+Requests (a scenario: rasters, forcing, simulated horizon) arrive over time.
+The server keeps every admitted scenario resident in one `Batch` and
+advances all of them together, a tick of `launches_per_tick` iterations at a
+time.  Between ticks it
+
+  * admits arrived requests in arrival order while their device footprint
+    fits the memory budget (a request that does not fit waits; smaller ones
+    behind it may pass it, so memory freed by one retirement is used at once),
+  * retires the scenarios whose plan has stopped (simulated horizon reached),
+    downloading their result (depth raster and FP64 budget),
+  * records per request: arrival, admission and completion times.
+
+Nothing here touches the numerics: each scenario advances exactly as it
+would alone (per-scenario clocks and CFL steps in the batched kernel).
+
+The backend is injected (`batch_factory`), so the scheduling logic is
+tested on the host with a fake batch.
+"""
+from __future__ import annotations
+
+import dataclasses
+import heapq
+import time
+from typing import Callable, Optional
+
+import numpy as np
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    arrival: float                 # seconds from the start of the run
+    cfg: object                    # sw2d Config (FP32, CFL)
+    z: np.ndarray
+    depth: np.ndarray
+    manning: Optional[np.ndarray]
+    rain_kind: int
+    rain: Optional[np.ndarray]
+    rain_dt: float
+    t_end: float                   # simulated horizon [s]
+    bytes: int = 0                 # device footprint in the batch
+    # filled by the server
+    admitted: Optional[float] = None
+    finished: Optional[float] = None
+    result: Optional[dict] = None
+
+
+class Server:
+    def __init__(self, batch_factory: Callable[[], object], bytes_of: Callable[[Request], int],
+                 max_bytes: int, launches_per_tick: int = 24, keep_results: bool = False,
+                 clock: Callable[[], float] = time.perf_counter, sleep: Callable[[float], None] = time.sleep):
+        self.batch = batch_factory()
+        self.bytes_of = bytes_of
+        self.max_bytes = int(max_bytes)
+        self.launches_per_tick = int(launches_per_tick)
+        self.keep_results = keep_results
+        self.clock = clock
+        self.sleep = sleep
+        self.pending: list = []         # heap of (arrival, rid, Request) not yet admitted
+        self.running: dict = {}         # scenario id -> Request
+        self.done: list = []
+        self.bytes_used = 0
+        self.peak_bytes = 0
+        self.ticks = 0
+        self.t0 = None
+
+    # ---- submission ----------------------------------------------------------
+    def submit(self, req: Request):
+        req.bytes = int(self.bytes_of(req))
+        if req.bytes > self.max_bytes:
+            raise ValueError(f"request {req.rid} needs {req.bytes} bytes, more than the budget {self.max_bytes}")
+        heapq.heappush(self.pending, (req.arrival, req.rid, req))
+
+    # ---- one scheduling round ------------------------------------------------
+    def now(self):
+        return self.clock() - self.t0
+
+    def _admit(self):
+        now = self.now()
+        waiting = []
+        while self.pending and self.pending[0][0] <= now:
+            waiting.append(heapq.heappop(self.pending))
+        for item in waiting:
+            req = item[2]
+            if self.bytes_used + req.bytes <= self.max_bytes:
+                sid = self.batch.add(req.cfg, req.z, req.depth, manning=req.manning, rain_kind=req.rain_kind,
+                                     rain=req.rain, rain_dt=req.rain_dt, t_end=req.t_end)
+                req.admitted = self.now()
+                self.running[sid] = req
+                self.bytes_used += req.bytes
+                self.peak_bytes = max(self.peak_bytes, self.bytes_used)
+            else:
+                heapq.heappush(self.pending, item)  # waits for memory, keeps its place
+
+    def _retire(self):
+        status = self.batch.poll()
+        for sid, st in status.items():
+            if sid in self.running and not st["running"]:
+                req = self.running.pop(sid)
+                res = {"t": st["t"], "steps": st["steps"], "budget": self.batch.budget(sid)}
+                if self.keep_results:
+                    res["depth"] = self.batch.field(sid)
+                req.result = res
+                req.finished = self.now()
+                self.batch.remove(sid)
+                self.bytes_used -= req.bytes
+                self.done.append(req)
+
+    def step(self):
+        """Admit, advance one tick if anything is resident, retire."""
+        self._admit()
+        if self.running:
+            self.batch.advance(self.launches_per_tick, wait=False)
+            self.ticks += 1
+            self._retire()
+            return True
+        return False
+
+    def run(self, requests=(), timeout=None):
+        """Serves `requests` (plus anything submitted before) until all are done."""
+        for r in requests:
+            self.submit(r)
+        self.t0 = self.clock()
+        while self.pending or self.running:
+            if timeout is not None and self.now() > timeout:
+                raise TimeoutError(f"{len(self.pending)} pending and {len(self.running)} running after {timeout} s")
+            if not self.step():
+                # idle: wait for the next arrival
+                nxt = self.pending[0][0] - self.now()
+                if nxt > 0:
+                    self.sleep(min(nxt, 0.05))
+        return self.stats()
+
+    def stats(self):
+        if not self.done:
+            return {"requests": 0}
+        ttr = np.array([r.finished - r.arrival for r in self.done])
+        span = max(r.finished for r in self.done) - min(r.arrival for r in self.done)
+        cu = sum(int(r.cfg.rows) * int(r.cfg.cols) * int(r.result["steps"]) for r in self.done)
+        return {
+            "requests": len(self.done),
+            "p50_s": float(np.percentile(ttr, 50)),
+            "p99_s": float(np.percentile(ttr, 99)),
+            "mean_s": float(ttr.mean()),
+            "scenarios_per_hour": len(self.done) / span * 3600.0 if span > 0 else None,
+            "cell_updates_per_s": cu / span if span > 0 else None,
+            "peak_bytes": int(self.peak_bytes),
+            "ticks": self.ticks,
+            "span_s": float(span),
+        }
+
+
+def poisson_arrivals(rate, n, seed):
+    """Arrival times of a Poisson process with `rate` per second."""
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    return np.cumsum(rng.exponential(1.0 / rate, size=n))

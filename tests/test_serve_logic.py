@@ -1,0 +1,115 @@
+"""The serving loop's scheduling on the host, with a fake batch: admission
+by footprint in arrival order, waiting for memory, retirement, statistics."""
+import numpy as np
+import pytest
+
+
+class FakeClock:
+    def __init__(self):
+        self.t = 0.0
+
+    def __call__(self):
+        return self.t
+
+    def sleep(self, dt):
+        self.t += dt
+
+
+class FakeBatch:
+    """Each scenario runs for `steps_needed` launches; time advances by
+    `tick_cost` per advance."""
+
+    def __init__(self, clock, tick_cost=0.1):
+        self.clock, self.tick_cost = clock, tick_cost
+        self.scen, self.next_id, self.adds, self.removes = {}, 0, [], []
+
+    def add(self, cfg, z, depth, manning=None, rain_kind=0, rain=None, rain_dt=1.0, t_end=1e300):
+        sid = self.next_id
+        self.next_id += 1
+        self.scen[sid] = {"left": int(t_end), "steps": 0}
+        self.adds.append((sid, self.clock.t))
+        return sid
+
+    def advance(self, launches, wait=True):
+        self.clock.t += self.tick_cost
+        for s in self.scen.values():
+            k = min(launches, s["left"])
+            s["left"] -= k
+            s["steps"] += k
+
+    def poll(self):
+        return {sid: {"running": s["left"] > 0, "t": float(s["steps"]), "steps": s["steps"]}
+                for sid, s in self.scen.items()}
+
+    def budget(self, sid):
+        return {"volume": 0.0}
+
+    def field(self, sid, which=0):
+        return np.zeros((1, 1))
+
+    def remove(self, sid):
+        self.removes.append((sid, self.clock.t))
+        del self.scen[sid]
+
+
+class Cfg:
+    rows = 10
+    cols = 10
+
+
+def _req(serve, rid, arrival, steps, nbytes):
+    r = serve.Request(rid=rid, arrival=arrival, cfg=Cfg(), z=None, depth=None, manning=None, rain_kind=0, rain=None,
+                      rain_dt=1.0, t_end=float(steps))
+    r._bytes = nbytes
+    return r
+
+
+def test_admission_respects_memory_and_order():
+    from sw2d import serve
+    clk = FakeClock()
+    fb = FakeBatch(clk)
+    srv = serve.Server(lambda: fb, bytes_of=lambda r: r._bytes, max_bytes=100, launches_per_tick=10, clock=clk,
+                       sleep=clk.sleep)
+    reqs = [_req(serve, 0, 0.0, 30, 60), _req(serve, 1, 0.0, 10, 60), _req(serve, 2, 0.0, 10, 30)]
+    st = srv.run(reqs)
+    assert st["requests"] == 3
+    assert srv.peak_bytes <= 100
+    # request 1 (60 B) cannot join request 0 (60 B); request 2 (30 B) can
+    first_tick = [sid for sid, t in fb.adds if t == 0.0]
+    assert first_tick == [0, 1] or first_tick == [0, 2]
+    admitted = {r.rid: r.admitted for r in srv.done}
+    assert admitted[0] == 0.0 and admitted[2] == 0.0 and admitted[1] > 0.0
+    for r in srv.done:
+        assert r.finished >= r.admitted >= r.arrival
+
+
+def test_requests_wait_for_arrival_and_stats():
+    from sw2d import serve
+    clk = FakeClock()
+    fb = FakeBatch(clk, tick_cost=0.05)
+    srv = serve.Server(lambda: fb, bytes_of=lambda r: 10, max_bytes=1000, launches_per_tick=5, clock=clk,
+                       sleep=clk.sleep)
+    arr = serve.poisson_arrivals(rate=4.0, n=20, seed=3)
+    reqs = [_req(serve, k, float(a), 20, 10) for k, a in enumerate(arr)]
+    st = srv.run(reqs)
+    assert st["requests"] == 20
+    for r in srv.done:
+        assert r.admitted >= r.arrival
+        assert r.result["steps"] == 20
+    assert 0 < st["p50_s"] <= st["p99_s"]
+    assert len(fb.scen) == 0 and srv.bytes_used == 0
+
+
+def test_oversized_request_rejected():
+    from sw2d import serve
+    clk = FakeClock()
+    srv = serve.Server(lambda: FakeBatch(clk), bytes_of=lambda r: 500, max_bytes=100, clock=clk, sleep=clk.sleep)
+    with pytest.raises(ValueError):
+        srv.submit(_req(serve, 0, 0.0, 5, 500))
+
+
+def test_poisson_arrivals_rate():
+    from sw2d import serve
+    a = serve.poisson_arrivals(rate=10.0, n=5000, seed=1)
+    assert np.all(np.diff(a) > 0)
+    assert abs(len(a) / a[-1] - 10.0) < 0.5
