@@ -30,6 +30,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "sw2d-gpu_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
