@@ -1,4 +1,5 @@
-"""Builds tests/golden/dam_break.npz from the reference's dam_break case.
+"""Builds tests/golden/dam_break.npz and tests/golden/dam_break_db.tar.gz
+from the reference's dam_break case.
 
 Run here, where the reference is mounted (it is not on the GPU machine):
 
@@ -9,14 +10,20 @@ and the reference's shipped output db/dam_break/output/Results_0.vtk, the one
 known-answer vector the reference ships: the first VTK written by its solver
 loop (SW2D-GPU.cu:1339-1472), i.e. depth = initial condition and velocities
 after ONE iteration.  Values are stored as the floats the VTK prints ("%f").
+
+dam_break_db.tar.gz holds the case's input files and that VTK byte for byte,
+for the end-to-end test of the reference-format driver.
 """
+import io
 import os
 import sys
+import tarfile
 
 import numpy as np
 
 DEFAULT = "/root/reference/SW2D-GPU_linux/src/db/dam_break"
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "dam_break.npz")
+OUT_DB = os.path.join(os.path.dirname(os.path.abspath(__file__)), "dam_break_db.tar.gz")
 
 
 def read_setup(path):
@@ -89,6 +96,16 @@ def main():
         vtk_y_velocity=vtk["y_velocity"], vtk_elevation=vtk["Elevations"],
     )
     print("wrote", OUT, {k: v.shape for k, v in vtk.items()})
+    with tarfile.open(OUT_DB, "w:gz") as tf:
+        for sub in ("input", "output"):
+            for fn in sorted(os.listdir(os.path.join(case, sub))):
+                path = os.path.join(case, sub, fn)
+                data = open(path, "rb").read()
+                info = tarfile.TarInfo(f"dam_break/{sub}/{fn}")
+                info.size = len(data)
+                info.mtime = 0
+                tf.addfile(info, io.BytesIO(data))
+    print("wrote", OUT_DB, os.path.getsize(OUT_DB), "bytes")
 
 
 if __name__ == "__main__":

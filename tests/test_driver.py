@@ -1,0 +1,67 @@
+"""The reference-format host driver (sw2d_run) end to end.
+
+The reference's own dam_break case (inputs and its shipped Results_0.vtk,
+tests/golden/dam_break_db.tar.gz) runs through the driver; the VTK the
+driver writes must equal the reference's byte for byte."""
+import os
+import subprocess
+import tarfile
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "dam_break_db.tar.gz")
+
+
+def _db(tmp_path):
+    with tarfile.open(GOLD) as tf:
+        tf.extractall(tmp_path / "db")
+    os.rename(tmp_path / "db" / "dam_break" / "output" / "Results_0.vtk", tmp_path / "reference_Results_0.vtk")
+    (tmp_path / "db" / "dir.txt").write_text("dir_number: 1\ndam_break\n")
+    return tmp_path / "db"
+
+
+def _driver(sw2d_mod):
+    import build_native
+    return build_native.DRIVER
+
+
+def test_driver_rejects_bad_arguments(sw2d_mod):
+    r = subprocess.run([_driver(sw2d_mod), "--bogus"], capture_output=True, text=True)
+    assert r.returncode == 2 and "usage" in r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_reproduces_reference_vtk_byte_for_byte(sw2d_mod, tmp_path):
+    db = _db(tmp_path)
+    r = subprocess.run([_driver(sw2d_mod), "--db", str(db), "--max-outputs", "1"], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    got = (db / "dam_break" / "output" / "Results_0.vtk").read_bytes()
+    ref = (tmp_path / "reference_Results_0.vtk").read_bytes()
+    assert got == ref
+    assert (db / "dam_break" / "output" / "WaterLevel.txt").read_text() == "Outlet off\n"
+    assert (db / "dam_break" / "output" / "TimeSimu_0.txt").exists()
+
+
+@pytest.mark.gpu
+def test_driver_second_output_matches_oracle(sw2d_mod, oracle_mod, tmp_path):
+    """The output at 60 s (mstep = lkout) against the oracle run on the
+    same inputs, compared at the VTK's printed precision."""
+    db = _db(tmp_path)
+    r = subprocess.run([_driver(sw2d_mod), "--db", str(db), "--max-outputs", "2"], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = db / "dam_break" / "output" / "Results_1.vtk"
+    assert out.exists() and not (db / "dam_break" / "output" / "Results_2.vtk").exists()
+    txt = out.read_text().split("\n")
+    k = txt.index("SCALARS depth float 1") + 2
+    depth = np.array([float(x) for x in txt[k:k + 10000]]).reshape(100, 100)[::-1]
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "dam_break.npz"))
+    o = oracle_mod.Oracle(100, 100, 10.0, 10.0, d["z"], manning=float(d["manning"]), INT=float(d["INT"]),
+                          INF=float(d["INF"]), LWL=float(d["LWL"]), EV_WL_min=float(d["EV_WL_min"]), dt_mode=0,
+                          dt=0.04)
+    o.set_state(d["h0"])
+    assert o.advance(750, 6000.0) == 750
+    ref = np.array([float("%f" % v) for v in o.state()["h"].ravel()]).reshape(100, 100)
+    assert np.array_equal(depth, ref)
