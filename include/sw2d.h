@@ -186,6 +186,16 @@ int sw2d_get_budget(sw2d_handle *h, sw2d_budget *out);
  * loop cu:1386-1410. */
 int sw2d_probe(sw2d_handle *h, const int32_t *cells, int32_t n, double *out);
 
+/* Checkpoint / restore (extension; the reference restarts only from a depth
+ * raster, cu:1022-1033).  A checkpoint holds the state in the working
+ * precision bit for bit (h, um, vn), the simulated time, the iteration count,
+ * the CFL bound and the FP64 budgets, so that a handle restored from it
+ * continues exactly as the one it was taken from.  It can be loaded into any
+ * handle created with the same config (after sw2d_set_static). */
+int sw2d_checkpoint_bytes(sw2d_handle *h, int64_t *bytes);
+int sw2d_checkpoint_save(sw2d_handle *h, void *buf, int64_t bytes);
+int sw2d_checkpoint_load(sw2d_handle *h, const void *buf, int64_t bytes);
+
 /* Waits for all work of the handle.  The stream (a cudaStream_t) is
  * exposed so that callers can order their own work or time it. */
 int sw2d_synchronize(sw2d_handle *h);

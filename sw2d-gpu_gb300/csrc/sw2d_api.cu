@@ -706,6 +706,93 @@ int sw2d_probe(sw2d_handle *h, const int32_t *cells, int32_t n, double *out) {
     return SW2D_OK;
 }
 
+namespace {
+struct CheckpointHeader {
+    char magic[8];  // "SW2DCKP1"
+    int32_t rows, cols, pitch, precision;
+    int64_t plane_bytes;
+    double volume0;
+    Clock clock;
+};
+}  // namespace
+
+int sw2d_checkpoint_bytes(sw2d_handle *h, int64_t *bytes) {
+    if (!h || !bytes) return SW2D_ERR_INVALID_ARG;
+    *bytes = (int64_t)(sizeof(CheckpointHeader) + 3 * h->plane * h->real_size);
+    return SW2D_OK;
+}
+
+int sw2d_checkpoint_save(sw2d_handle *h, void *buf, int64_t bytes) {
+    int64_t need = 0;
+    if (!h || !buf) return fail(h, SW2D_ERR_INVALID_ARG, "null argument");
+    sw2d_checkpoint_bytes(h, &need);
+    if (bytes < need) return fail(h, SW2D_ERR_INVALID_ARG, "checkpoint buffer too small");
+    if (!h->have_state) return fail(h, SW2D_ERR_STATE, "no state");
+    int rc = read_clock(h);
+    if (rc) return rc;
+    CheckpointHeader hd;
+    std::memset(&hd, 0, sizeof(hd));
+    std::memcpy(hd.magic, "SW2DCKP1", 8);
+    hd.rows = h->cfg.rows;
+    hd.cols = h->cfg.cols;
+    hd.pitch = h->pitch;
+    hd.precision = h->cfg.precision;
+    hd.plane_bytes = (int64_t)(h->plane * h->real_size);
+    hd.volume0 = h->volume0;
+    hd.clock = h->clock;
+    char *p = static_cast<char *>(buf);
+    std::memcpy(p, &hd, sizeof(hd));
+    p += sizeof(hd);
+    const int b = h->clock.buf;
+    void *src[3] = {h->h[b], h->um[b], h->vn[b]};
+    for (int k = 0; k < 3; k++) {
+        CK(h, cudaMemcpyAsync(p, src[k], (size_t)hd.plane_bytes, cudaMemcpyDeviceToHost, h->stream));
+        p += hd.plane_bytes;
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    return SW2D_OK;
+}
+
+int sw2d_checkpoint_load(sw2d_handle *h, const void *buf, int64_t bytes) {
+    if (!h || !buf) return fail(h, SW2D_ERR_INVALID_ARG, "null argument");
+    if (!h->have_static) return fail(h, SW2D_ERR_STATE, "sw2d_set_static must come first");
+    if (bytes < (int64_t)sizeof(CheckpointHeader)) return fail(h, SW2D_ERR_INVALID_ARG, "not a checkpoint");
+    CheckpointHeader hd;
+    std::memcpy(&hd, buf, sizeof(hd));
+    int64_t need = 0;
+    sw2d_checkpoint_bytes(h, &need);
+    if (std::memcmp(hd.magic, "SW2DCKP1", 8) != 0 || hd.rows != h->cfg.rows || hd.cols != h->cfg.cols ||
+        hd.pitch != h->pitch || hd.precision != h->cfg.precision || bytes < need)
+        return fail(h, SW2D_ERR_INVALID_ARG, "checkpoint does not match this handle's config");
+    const char *p = static_cast<const char *>(buf) + sizeof(hd);
+    void *dst[3] = {h->h[0], h->um[0], h->vn[0]};
+    for (int k = 0; k < 3; k++) {
+        CK(h, cudaMemcpyAsync(dst[k], p, (size_t)hd.plane_bytes, cudaMemcpyHostToDevice, h->stream));
+        p += hd.plane_bytes;
+    }
+    const size_t fb = h->plane * h->real_size;
+    CK(h, cudaMemsetAsync(h->h[1], 0, fb, h->stream));
+    CK(h, cudaMemsetAsync(h->um[1], 0, fb, h->stream));
+    CK(h, cudaMemsetAsync(h->vn[1], 0, fb, h->stream));
+    // the saved clock becomes slot 0 of a fresh launch sequence
+    Clock c = hd.clock;
+    c.buf = 0;
+    c.cmax_bits = hd.clock.cmax_bits;
+    c.done_blocks = 0;
+    for (int q = 0; q < B_N; q++)
+        for (int bb = 0; bb < kBuckets; bb++) c.stepb[q][bb] = 0.0;
+    for (int bb = 0; bb < kBuckets; bb++) c.cmaxb[bb] = 0ull;
+    CK(h, cudaMemsetAsync(h->d_clk, 0, 3 * sizeof(Clock), h->stream));
+    *h->h_clk = c;
+    CK(h, cudaMemcpyAsync(h->d_clk, h->h_clk, sizeof(Clock), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->launches = 0;
+    h->clock = c;
+    h->volume0 = hd.volume0;
+    h->have_state = true;
+    return SW2D_OK;
+}
+
 int sw2d_synchronize(sw2d_handle *h) {
     if (!h) return SW2D_ERR_INVALID_ARG;
     CK(h, cudaStreamSynchronize(h->stream));

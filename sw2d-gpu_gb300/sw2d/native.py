@@ -86,6 +86,9 @@ _SIGS = {
     "sw2d_status_string": (C.c_char_p, [C.c_int32]),
     "sw2d_volume_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_double,
                                       C.c_void_p, C.POINTER(C.c_double)]),
+    "sw2d_checkpoint_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "sw2d_checkpoint_save": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "sw2d_checkpoint_load": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     "sw2d_batch_config_init": (C.c_int, [C.POINTER(BatchConfig)]),
     "sw2d_batch_scenario_bytes": (C.c_int, [C.POINTER(Config), C.c_int32, C.c_int32, C.POINTER(C.c_int64)]),
     "sw2d_batch_create": (C.c_int, [C.POINTER(BatchConfig), C.POINTER(C.c_void_p)]),
@@ -262,6 +265,17 @@ class Solver:
         b = Budget()
         self._check(load().sw2d_get_budget(self._h, C.byref(b)), "sw2d_get_budget")
         return {k: getattr(b, k) for k, _ in Budget._fields_ if k != "reserved"}
+
+    def checkpoint(self) -> bytes:
+        """Bit-exact snapshot of the resident state, time, step count and budgets."""
+        n = C.c_int64()
+        self._check(load().sw2d_checkpoint_bytes(self._h, C.byref(n)), "sw2d_checkpoint_bytes")
+        buf = C.create_string_buffer(n.value)
+        self._check(load().sw2d_checkpoint_save(self._h, buf, n.value), "sw2d_checkpoint_save")
+        return buf.raw
+
+    def restore(self, ckpt: bytes):
+        self._check(load().sw2d_checkpoint_load(self._h, ckpt, len(ckpt)), "sw2d_checkpoint_load")
 
     def probe(self, cells):
         cells = np.ascontiguousarray(cells, dtype=np.int32)
