@@ -121,9 +121,11 @@ int upload_units(sw2d_batch *b) {
     return SW2D_OK;
 }
 
-int strip_for(const sw2d_batch *b, int rows) {
+// rows per warp: the scenario's own setting (autotuned), the batch's, or by size
+int strip_for(const sw2d_batch *b, const sw2d_config *c) {
+    if (c->strip_h > 0) return c->strip_h;
     if (b->cfg.strip_h > 0) return b->cfg.strip_h;
-    return rows >= 1024 ? 64 : (rows >= 256 ? 32 : 16);
+    return c->rows >= 1024 ? 64 : (c->rows >= 256 ? 32 : 16);
 }
 
 template <class T>
@@ -257,7 +259,7 @@ int sw2d_batch_add(sw2d_batch *b, const sw2d_config *cfg, const double *z, const
     h.cfg = *cfg;
     h.raster = raster;
     h.pitch = ((cfg->cols + 1 + 31) / 32) * 32;
-    h.strip_h = strip_for(b, cfg->rows);
+    h.strip_h = strip_for(b, cfg);
     h.tiles_w = (cfg->cols + stream_out_cols() - 1) / stream_out_cols();
     h.nunits = h.tiles_w * ((cfg->rows + h.strip_h - 1) / h.strip_h);
     BCK(b, cudaSetDevice(b->cfg.device));

@@ -1,0 +1,142 @@
+"""Autotuner for the FP32 streaming kernel: tile shape and launches per sync.
+
+For a grid-size class it times every candidate (strip height, kernel build)
+on a wet synthetic catchment of that size and keeps the fastest, then times
+the CUDA-graph chunk (iterations replayed between host synchronisations) for
+batched runs.  Results are cached in a JSON file keyed by GPU name and size
+class, so a tuning run is paid once per machine.
+
+    from sw2d import autotune
+    best = autotune.tune(2048, 2048)          # {"strip_h": 48, "variant": 0, ...}
+    cfg = autotune.apply(cfg)                 # fills strip_h/variant from the cache
+"""
+from __future__ import annotations
+
+import json
+import os
+import time
+from typing import Callable, Optional
+
+import numpy as np
+
+STRIPS = (16, 24, 32, 48, 64, 96, 128)
+VARIANTS = (0, 1, 2, 3, 4, 5)
+CHUNKS = (12, 24, 48, 96)
+
+
+def default_cache_path() -> str:
+    base = os.environ.get("XDG_CACHE_HOME", os.path.join(os.path.expanduser("~"), ".cache"))
+    return os.path.join(base, "sw2d", "autotune.json")
+
+
+def size_class(rows: int, cols: int) -> str:
+    """Grids within a factor sqrt(2) in cell count share a class."""
+    return f"c{int(round(2 * np.log2(max(rows * cols, 1))))}"
+
+
+class Cache:
+    def __init__(self, path: Optional[str] = None):
+        self.path = path or default_cache_path()
+        self.data = {}
+        if os.path.exists(self.path):
+            try:
+                with open(self.path) as f:
+                    self.data = json.load(f)
+            except (OSError, ValueError):
+                self.data = {}
+
+    def get(self, gpu: str, cls: str):
+        return self.data.get(gpu, {}).get(cls)
+
+    def put(self, gpu: str, cls: str, entry: dict):
+        self.data.setdefault(gpu, {})[cls] = entry
+        os.makedirs(os.path.dirname(self.path) or ".", exist_ok=True)
+        tmp = self.path + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(self.data, f, indent=1, sort_keys=True)
+        os.replace(tmp, self.path)
+
+
+def gpu_name(device: int = 0) -> str:
+    try:
+        import torch
+        return torch.cuda.get_device_name(device)
+    except Exception:
+        return "unknown-gpu"
+
+
+def search(candidates, timer: Callable[[dict], float]):
+    """Times every candidate (seconds per iteration, lower is better) and
+    returns (best candidate, table of timings)."""
+    table = []
+    for c in candidates:
+        try:
+            t = float(timer(c))
+        except Exception as e:  # a candidate that cannot run is skipped
+            table.append({**c, "error": str(e)})
+            continue
+        table.append({**c, "s_per_iter": t})
+    ok = [r for r in table if "s_per_iter" in r]
+    if not ok:
+        raise RuntimeError("no autotuning candidate ran")
+    best = min(ok, key=lambda r: r["s_per_iter"])
+    return {k: v for k, v in best.items() if k != "s_per_iter"}, table
+
+
+def _kernel_timer(rows, cols, device, iters):
+    import sw2d
+    from sw2d import scenarios as S
+    s = S.catchment(rows, dx=5.0, seed=1, cols=cols)
+    h0 = np.full((rows, cols), 0.005)
+
+    def timer(c):
+        g = sw2d.Solver(rows=rows, cols=cols, dx=5.0, dy=5.0, precision=sw2d.PREC_F32, dt_mode=sw2d.DT_CFL, dt=1.0,
+                        cfl=0.5, south_open=1, kernel=sw2d.KERNEL_STREAM, strip_h=c["strip_h"],
+                        variant=c["variant"], device=device)
+        try:
+            g.set_static(s["z"], s["n"])
+            g.set_rain(sw2d.RAIN_STEP, [50.0], 3600.0)
+            g.set_state(h0)
+            g.advance(6)
+            g.synchronize()
+            t0 = time.perf_counter()
+            n = g.advance(iters)
+            g.synchronize()
+            return (time.perf_counter() - t0) / max(n, 1)
+        finally:
+            g.close()
+    return timer
+
+
+def tune(rows: int, cols: int, device: int = 0, cache: Optional[Cache] = None, iters: int = 48,
+         strips=STRIPS, variants=VARIANTS, force: bool = False) -> dict:
+    """Best (strip_h, variant) for a rows x cols grid on this GPU (cached)."""
+    cache = cache or Cache()
+    gpu, cls = gpu_name(device), size_class(rows, cols)
+    hit = cache.get(gpu, cls)
+    if hit and not force:
+        return hit
+    cands = [{"strip_h": sh, "variant": v} for v in variants for sh in strips if sh <= max(rows, 16)]
+    best, table = search(cands, _kernel_timer(rows, cols, device, iters))
+    entry = {**best, "rows": rows, "cols": cols, "timings": table}
+    cache.put(gpu, cls, entry)
+    return entry
+
+
+def apply(cfg, cache: Optional[Cache] = None, device: int = 0):
+    """Fills cfg.strip_h / cfg.variant from the cache (FP32 only); returns cfg."""
+    import sw2d
+    if cfg.precision != sw2d.PREC_F32:
+        return cfg
+    hit = (cache or Cache()).get(gpu_name(device), size_class(cfg.rows, cfg.cols))
+    if hit:
+        cfg.strip_h = int(hit["strip_h"])
+        cfg.variant = int(hit["variant"])
+    return cfg
+
+
+def tune_chunk(batch_runner: Callable[[int], float], chunks=CHUNKS) -> dict:
+    """Graph chunk (iterations between host synchronisations) for a batch:
+    `batch_runner(chunk)` returns seconds per iteration for that chunk."""
+    best, table = search([{"chunk": c} for c in chunks], lambda c: batch_runner(c["chunk"]))
+    return {**best, "timings": table}
