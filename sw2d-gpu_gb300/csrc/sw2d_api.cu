@@ -35,7 +35,8 @@ struct sw2d_handle {
     sw2d_config cfg{};
     int real_size = 8;
     int pitch = 0;
-    size_t plane = 0;  // elements per pitched array: (rows+1) * pitch
+    size_t plane = 0;   // elements per allocated array, frame included
+    size_t origin = 0;  // element offset of cell (0,0) in an allocation
     int tile_h = 16, tile_w = 32, nblocks = 0;
     bool stream_kernel = false;  // FP32 warp-streaming kernel instead of the tile kernel
     int strip_h = 0, stream_tiles_w = 0, stream_units = 0, variant = 0;
@@ -82,6 +83,9 @@ int cuda_fail(sw2d_handle *h, cudaError_t e, const char *what) {
     } while (0)
 
 bool is_f64(const sw2d_handle *h) { return h->cfg.precision == SW2D_PREC_F64; }
+
+// start of the allocation of a state field (its frame included)
+void *raw_field(const sw2d_handle *h, void *p) { return static_cast<char *>(p) - h->origin * h->real_size; }
 
 template <class Real>
 Real thr_ge(double x) {
@@ -152,8 +156,8 @@ int validate(const sw2d_config *c, std::string *why) {
 }
 
 void grid_shape(const sw2d_config *c, int *pitch, size_t *plane, int *th, int *tw) {
-    *pitch = ((c->cols + 1 + 31) / 32) * 32;
-    *plane = (size_t)(c->rows + 1) * (size_t)(*pitch);
+    *pitch = pitch_for(c->cols);
+    *plane = plane_for(c->rows, *pitch);
     int a = c->tile_h, b = c->tile_w;
     if (a <= 0 || b <= 0 || !tile_supported(c->precision, a, b)) default_tile(c->precision, &a, &b);
     *th = a;
@@ -261,7 +265,7 @@ int sw2d_device_bytes(const sw2d_config *c, int64_t *bytes) {
     size_t plane;
     grid_shape(c, &pitch, &plane, &th, &tw);
     const size_t rs = c->precision == SW2D_PREC_F64 ? 8 : 4;
-    size_t total = plane * rs * 8;  // 2x(h, um, vn) + z + n
+    size_t total = plane * rs * 8;  // 2x(h, um, vn) + z + n, frame included
     total += plane;                 // mask
     total += 2 * (size_t)(c->rows + 1) * (c->cols + 1) * sizeof(double);  // staging
     total += kVolumeBlocks * sizeof(double) + 3 * sizeof(Clock) + sizeof(Control);
@@ -278,6 +282,7 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
     h->cfg = *cfg;
     h->real_size = cfg->precision == SW2D_PREC_F64 ? 8 : 4;
     grid_shape(cfg, &h->pitch, &h->plane, &h->tile_h, &h->tile_w);
+    h->origin = origin_for(h->pitch);
     auto bail = [&](int code) {
         sw2d_destroy(h);
         return code;
@@ -286,17 +291,23 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
     if (e != cudaSuccess) return bail(SW2D_ERR_CUDA);
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(SW2D_ERR_CUDA);
     const size_t fb = h->plane * h->real_size;
+    // allocate with the zero frame, keep pointers at cell (0,0)
+    auto alloc_field = [&](void **p, size_t esz) -> bool {
+        void *raw = nullptr;
+        if (cudaMalloc(&raw, h->plane * esz) != cudaSuccess) return false;
+        if (cudaMemset(raw, 0, h->plane * esz) != cudaSuccess) return false;
+        *p = static_cast<char *>(raw) + h->origin * esz;
+        return true;
+    };
     for (int b = 0; b < 2; b++) {
         void **arrs[3] = {&h->h[b], &h->um[b], &h->vn[b]};
-        for (void **a : arrs) {
-            if (cudaMalloc(a, fb) != cudaSuccess) return bail(SW2D_ERR_OOM);
-            if (cudaMemset(*a, 0, fb) != cudaSuccess) return bail(SW2D_ERR_CUDA);
-        }
+        for (void **a : arrs)
+            if (!alloc_field(a, h->real_size)) return bail(SW2D_ERR_OOM);
     }
-    if (cudaMalloc(&h->z, fb) != cudaSuccess || cudaMemset(h->z, 0, fb) != cudaSuccess) return bail(SW2D_ERR_OOM);
-    if (cudaMalloc(&h->nman, fb) != cudaSuccess || cudaMemset(h->nman, 0, fb) != cudaSuccess) return bail(SW2D_ERR_OOM);
-    if (cudaMalloc((void **)&h->mask, h->plane) != cudaSuccess || cudaMemset(h->mask, 0, h->plane) != cudaSuccess)
+    if (!alloc_field(&h->z, h->real_size) || !alloc_field(&h->nman, h->real_size) ||
+        !alloc_field((void **)&h->mask, 1))
         return bail(SW2D_ERR_OOM);
+    (void)fb;
     h->stage_elems = (size_t)(cfg->rows + 1) * (cfg->cols + 1);
     if (cudaMalloc((void **)&h->stage, h->stage_elems * sizeof(double)) != cudaSuccess) return bail(SW2D_ERR_OOM);
     if (cudaMalloc((void **)&h->stage2, h->stage_elems * sizeof(double)) != cudaSuccess) return bail(SW2D_ERR_OOM);
@@ -375,14 +386,17 @@ int sw2d_destroy(sw2d_handle *h) {
     if (!h) return SW2D_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->graph) cudaGraphExecDestroy(h->graph);
+    auto free_field = [&](void *p, size_t esz) {
+        if (p) cudaFree(static_cast<char *>(p) - h->origin * esz);
+    };
     for (int b = 0; b < 2; b++) {
-        cudaFree(h->h[b]);
-        cudaFree(h->um[b]);
-        cudaFree(h->vn[b]);
+        free_field(h->h[b], h->real_size);
+        free_field(h->um[b], h->real_size);
+        free_field(h->vn[b], h->real_size);
     }
-    cudaFree(h->z);
-    cudaFree(h->nman);
-    cudaFree(h->mask);
+    free_field(h->z, h->real_size);
+    free_field(h->nman, h->real_size);
+    free_field(h->mask, 1);
     cudaFree(h->stage);
     cudaFree(h->stage2);
     cudaFree(h->partial);
@@ -427,9 +441,9 @@ int sw2d_set_state(sw2d_handle *h, const double *depth, const double *um, const 
     const int rows = h->cfg.rows, cols = h->cfg.cols, pitch = h->pitch;
     const size_t fb = h->plane * h->real_size;
     for (int b = 0; b < 2; b++) {
-        CK(h, cudaMemsetAsync(h->h[b], 0, fb, h->stream));
-        CK(h, cudaMemsetAsync(h->um[b], 0, fb, h->stream));
-        CK(h, cudaMemsetAsync(h->vn[b], 0, fb, h->stream));
+        CK(h, cudaMemsetAsync(raw_field(h, h->h[b]), 0, fb, h->stream));
+        CK(h, cudaMemsetAsync(raw_field(h, h->um[b]), 0, fb, h->stream));
+        CK(h, cudaMemsetAsync(raw_field(h, h->vn[b]), 0, fb, h->stream));
     }
     CK(h, cudaMemcpyAsync(h->stage, depth, (size_t)rows * cols * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     if (is_f64(h)) CK(h, launch_pack_depth(h->stage, rows, cols, pitch, h->mask, (double *)h->h[0], h->stream));
@@ -744,7 +758,7 @@ int sw2d_checkpoint_save(sw2d_handle *h, void *buf, int64_t bytes) {
     std::memcpy(p, &hd, sizeof(hd));
     p += sizeof(hd);
     const int b = h->clock.buf;
-    void *src[3] = {h->h[b], h->um[b], h->vn[b]};
+    void *src[3] = {raw_field(h, h->h[b]), raw_field(h, h->um[b]), raw_field(h, h->vn[b])};
     for (int k = 0; k < 3; k++) {
         CK(h, cudaMemcpyAsync(p, src[k], (size_t)hd.plane_bytes, cudaMemcpyDeviceToHost, h->stream));
         p += hd.plane_bytes;
@@ -765,15 +779,15 @@ int sw2d_checkpoint_load(sw2d_handle *h, const void *buf, int64_t bytes) {
         hd.pitch != h->pitch || hd.precision != h->cfg.precision || bytes < need)
         return fail(h, SW2D_ERR_INVALID_ARG, "checkpoint does not match this handle's config");
     const char *p = static_cast<const char *>(buf) + sizeof(hd);
-    void *dst[3] = {h->h[0], h->um[0], h->vn[0]};
+    void *dst[3] = {raw_field(h, h->h[0]), raw_field(h, h->um[0]), raw_field(h, h->vn[0])};
     for (int k = 0; k < 3; k++) {
         CK(h, cudaMemcpyAsync(dst[k], p, (size_t)hd.plane_bytes, cudaMemcpyHostToDevice, h->stream));
         p += hd.plane_bytes;
     }
     const size_t fb = h->plane * h->real_size;
-    CK(h, cudaMemsetAsync(h->h[1], 0, fb, h->stream));
-    CK(h, cudaMemsetAsync(h->um[1], 0, fb, h->stream));
-    CK(h, cudaMemsetAsync(h->vn[1], 0, fb, h->stream));
+    CK(h, cudaMemsetAsync(raw_field(h, h->h[1]), 0, fb, h->stream));
+    CK(h, cudaMemsetAsync(raw_field(h, h->um[1]), 0, fb, h->stream));
+    CK(h, cudaMemsetAsync(raw_field(h, h->vn[1]), 0, fb, h->stream));
     // the saved clock becomes slot 0 of a fresh launch sequence
     Clock c = hd.clock;
     c.buf = 0;

@@ -136,8 +136,8 @@ T *carve(char *base, size_t &off, size_t n) {
 }
 
 size_t scenario_bytes(const sw2d_config *c, int n_rain, bool raster) {
-    const int pitch = ((c->cols + 1 + 31) / 32) * 32;
-    const size_t plane = (size_t)(c->rows + 1) * pitch;
+    const int pitch = pitch_for(c->cols);
+    const size_t plane = plane_for(c->rows, pitch);
     size_t s = 0;
     s += 6 * align256(plane * sizeof(float));                    // h, um, vn x 2
     s += align256(plane * sizeof(float));                        // z
@@ -258,7 +258,7 @@ int sw2d_batch_add(sw2d_batch *b, const sw2d_config *cfg, const double *z, const
     h = HostScenario();
     h.cfg = *cfg;
     h.raster = raster;
-    h.pitch = ((cfg->cols + 1 + 31) / 32) * 32;
+    h.pitch = pitch_for(cfg->cols);
     h.strip_h = strip_for(b, cfg);
     h.tiles_w = (cfg->cols + stream_out_cols() - 1) / stream_out_cols();
     h.nunits = h.tiles_w * ((cfg->rows + h.strip_h - 1) / h.strip_h);
@@ -266,17 +266,18 @@ int sw2d_batch_add(sw2d_batch *b, const sw2d_config *cfg, const double *z, const
     BCK(b, cudaMallocAsync(&h.block, need, b->stream));
     h.bytes = need;
     b->bytes_in_use += (int64_t)need;
-    const size_t plane = (size_t)(cfg->rows + 1) * h.pitch;
+    const size_t plane = plane_for(cfg->rows, h.pitch), org = origin_for(h.pitch);
     char *base = static_cast<char *>(h.block);
     size_t off = 0;
     ScenarioDev &d = h.dev;
     std::memset(&d, 0, sizeof(d));
-    for (int k = 0; k < 2; k++) d.h[k] = carve<float>(base, off, plane);
-    for (int k = 0; k < 2; k++) d.um[k] = carve<float>(base, off, plane);
-    for (int k = 0; k < 2; k++) d.vn[k] = carve<float>(base, off, plane);
-    float *z_dev = carve<float>(base, off, plane);
-    float *n_dev = raster ? carve<float>(base, off, plane) : nullptr;
-    uint8_t *m_dev = carve<uint8_t>(base, off, plane);
+    // fields with their zero frame; pointers at cell (0,0)
+    for (int k = 0; k < 2; k++) d.h[k] = carve<float>(base, off, plane) + org;
+    for (int k = 0; k < 2; k++) d.um[k] = carve<float>(base, off, plane) + org;
+    for (int k = 0; k < 2; k++) d.vn[k] = carve<float>(base, off, plane) + org;
+    float *z_dev = carve<float>(base, off, plane) + org;
+    float *n_dev = raster ? carve<float>(base, off, plane) + org : nullptr;
+    uint8_t *m_dev = carve<uint8_t>(base, off, plane) + org;
     Clock *clk = carve<Clock>(base, off, 3);
     double *rain_dev = carve<double>(base, off, (size_t)(n_rain > 0 ? n_rain : 1));
     BCK(b, cudaMemsetAsync(h.block, 0, off, b->stream));

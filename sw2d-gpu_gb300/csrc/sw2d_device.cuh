@@ -471,9 +471,10 @@ __device__ __forceinline__ bool dry_bed(const Thr<Real> &T, Real g, Real ha, Rea
         q = (hb >= T.gt_th) ? Real(-0.544) * hb * RT<Real>::sqrt_(g * hb) : Real(0);
         return true;
     }
-    // cu:149: (hb - th) * (ha - th) < 0, i.e. exactly one side strictly wet
+    // cu:149: (hb - th) * (ha - th) < 0, i.e. exactly one side strictly wet;
+    // written with comparisons that are false for NaN, as the product is
     const bool b_wet = hb >= T.gt_th, a_wet = ha >= T.gt_th;
-    const bool b_dry = !(hb >= T.ge_th), a_dry = !(ha >= T.ge_th);
+    const bool b_dry = hb < T.ge_th, a_dry = ha < T.ge_th;
     if ((b_wet && a_dry) || (b_dry && a_wet)) {
         if ((hb > Real(0)) || (ha > Real(0))) {
             // -sgn(hb - ha) * 0.350 with sgn from the wet side (cu:151-154)
@@ -693,7 +694,7 @@ __global__ void __launch_bounds__(NT)
                         }
                         const Real rn = has_n ? Real(0.5) * (s_n[p] + s_n[pa]) : manning;
                         Real ram = 0;
-                        if ((hm >= T.gt_th) && rn != Real(0)) {  // cu:194-199
+                        if (!(hm < T.gt_th) && rn != Real(0)) {  // cu:194-199: zero only when hm <= th
                             const Real vva = Real(0.250) * (s_vv1[p] + s_vv1[p + 1] + s_vv1[pa] + s_vv1[pa + 1]);
                             const Real sqx = RT<Real>::sqrt_(uu_c * uu_c + vva * vva);
                             ram = g * rn * rn * sqx / RT<Real>::pow_(hm);
@@ -738,7 +739,7 @@ __global__ void __launch_bounds__(NT)
                     const Real v12 = dt2dy * (vnu - vnd);  // cu:307
                     const Real rn = has_n ? Real(0.5) * (s_n[p] + s_n[pa]) : manning;
                     Real ram = 0;
-                    if ((hn >= T.gt_th) && rn != Real(0)) {  // cu:311-316
+                    if (!(hn < T.gt_th) && rn != Real(0)) {  // cu:311-316: zero only when hn <= th
                         const Real uua = Real(0.250) * (s_uu1[p] + s_uu1[p + RW] + s_uu1[p - 1] + s_uu1[p + RW - 1]);
                         const Real sqy = RT<Real>::sqrt_(uua * uua + vv_c * vv_c);
                         ram = g * rn * rn * sqy / RT<Real>::pow_(hn);
@@ -788,14 +789,14 @@ __global__ void __launch_bounds__(NT)
     // corrected x-face at p: zero if it drains a dry cell
     auto fix_x = [&](int p) -> Real {
         const Real q = s_rum[p];
-        if (q > Real(0) && s_m[p - RW] && !(s_hs[p - RW] >= T.ge_th)) return Real(0);
-        if (q < Real(0) && s_m[p] && !(s_hs[p] >= T.ge_th)) return Real(0);
+        if (q > Real(0) && s_m[p - RW] && s_hs[p - RW] < T.ge_th) return Real(0);
+        if (q < Real(0) && s_m[p] && s_hs[p] < T.ge_th) return Real(0);
         return q;
     };
     auto fix_y = [&](int p) -> Real {
         const Real q = s_rvn[p];
-        if (q > Real(0) && s_m[p - 1] && !(s_hs[p - 1] >= T.ge_th)) return Real(0);
-        if (q < Real(0) && s_m[p] && !(s_hs[p] >= T.ge_th)) return Real(0);
+        if (q > Real(0) && s_m[p - 1] && s_hs[p - 1] < T.ge_th) return Real(0);
+        if (q < Real(0) && s_m[p] && s_hs[p] < T.ge_th) return Real(0);
         return q;
     };
 

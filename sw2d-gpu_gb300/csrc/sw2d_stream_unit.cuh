@@ -117,20 +117,22 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         return V.GS.storm_amp * __expf(-(x * x + y * y) / V.GS.storm_2s2);
     };
 
-    // row loads (zero outside the domain: inactive cells, walls)
+    // row loads: rows R0-4 .. R1+2 and columns gj0 .. gj0+31 all lie inside
+    // the zero frame around the domain, whose zeros are the inactive-cell and
+    // wall values, so no load needs a bounds test
     float p_h, p_z, p_n, p_um, p_vn;
     unsigned p_m;
-    auto load_row = [&](int r) {
-        const bool rc = (unsigned)r < (unsigned)rows;
-        const size_t gp = (size_t)r * pitch + gj;
-        const bool cell = rc && col_cell;
-        p_h = cell ? Hin[gp] : 0.f;
-        p_z = cell ? Zin[gp] : 0.f;
-        p_n = (cell && raster) ? Nin[gp] : manning;
-        p_m = cell ? (unsigned)Min[gp] : 0u;
-        p_um = ((unsigned)r <= (unsigned)rows && col_cell) ? Uin[gp] : 0.f;
-        p_vn = (rc && col_vn) ? Vin[gp] : 0.f;
+    long long gp = (long long)(R0 - 4) * pitch + gj;  // element offset of the next row to read
+    auto load_row = [&]() {
+        p_h = Hin[gp];
+        p_z = Zin[gp];
+        p_n = raster ? Nin[gp] : manning;
+        p_m = (unsigned)Min[gp];
+        p_um = Uin[gp];
+        p_vn = Vin[gp];
+        gp += pitch;
     };
+    (void)col_vn;
 
     // register rings: suffix = rows back from the row being read (r)
     float h1 = 0.f, h2 = 0.f, h3 = 0.f, hL1 = 0.f;
@@ -144,14 +146,14 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     unsigned mb = 0u, mLb = 0u;  // bit k: active mask of row r-k (own / west column)
 
     const int r_first = R0 - 4, r_last = R1 + 3;
-    load_row(r_first);
+    load_row();
 #pragma unroll 1
     for (int r = r_first; r < r_last; r++) {
         const float h0 = p_h, z0 = p_z, n0 = p_n, um0 = p_um, vn0 = p_vn;
         mb = (mb << 1) | p_m;
         const unsigned mL0 = __shfl_up_sync(0xffffffffu, p_m, 1);
         mLb = (mLb << 1) | mL0;
-        if (r + 1 < r_last) load_row(r + 1);  // prefetch
+        if (r + 1 < r_last) load_row();  // prefetch the next row
 
         const float hL0 = shup(h0), zL0 = shup(z0);
         const float nL0 = raster ? shup(n0) : manning;
@@ -187,7 +189,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
                         }
                         const float rn = 0.5f * (n1 + n2);
                         float ram = 0.f;
-                        if ((hm >= gt_th) && rn != 0.f) {  // cu:194-199
+                        if (!(hm < gt_th) && rn != 0.f) {  // cu:194-199: zero only when hm <= th
                             const float vva = 0.250f * (vv_1 + vvR_1 + vv_2 + vvR_2);
                             ram = g * rn * rn * sqrtf(uu_1 * uu_1 + vva * vva) / RT<float>::pow_(hm);
                         }
@@ -217,7 +219,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
                     const float v12 = dt2dy * (upwind<float>(v12vvu, vnE, vn1) - upwind_r<float>(v12vvd, vnW, vn1));
                     const float rn = 0.5f * (n1 + nL1);
                     float ram = 0.f;
-                    if ((hn >= gt_th) && rn != 0.f) {  // cu:311-316
+                    if (!(hn < gt_th) && rn != 0.f) {  // cu:311-316: zero only when hn <= th
                         const float uua = 0.250f * (uu_1 + uu_0 + uuL_1 + uuL_0);
                         ram = g * rn * rn * sqrtf(uua * uua + vv_1 * vv_1) / RT<float>::pow_(hn);
                     }
@@ -244,11 +246,11 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         const float hsW_3 = shup(hs_3);
         const bool m3 = (mb >> 3) & 1u, m4 = (mb >> 4) & 1u, m2 = (mb >> 2) & 1u, mL3 = (mLb >> 3) & 1u;
         float un = rum_3;  // x-face north of the row-(r-3) cell
-        if ((un > 0.f && m4 && !(hs_4 >= ge_th)) || (un < 0.f && m3 && !(hs_3 >= ge_th))) un = 0.f;
+        if ((un > 0.f && m4 && hs_4 < ge_th) || (un < 0.f && m3 && hs_3 < ge_th)) un = 0.f;
         float us = rum_2;  // x-face south of it
-        if ((us > 0.f && m3 && !(hs_3 >= ge_th)) || (us < 0.f && m2 && !(hs_2 >= ge_th))) us = 0.f;
+        if ((us > 0.f && m3 && hs_3 < ge_th) || (us < 0.f && m2 && hs_2 < ge_th)) us = 0.f;
         float vw = rvn_3;  // y-face west of it
-        if ((vw > 0.f && mL3 && !(hsW_3 >= ge_th)) || (vw < 0.f && m3 && !(hs_3 >= ge_th))) vw = 0.f;
+        if ((vw > 0.f && mL3 && hsW_3 < ge_th) || (vw < 0.f && m3 && hs_3 < ge_th)) vw = 0.f;
         const float ve = shdn(vw);
         const int f = r - 3;
         float hw_3 = 0.f, hraw = 0.f, rr1 = 0.f, pct1 = 0.f, ev1 = 0.f, ql1 = 0.f;

@@ -57,3 +57,16 @@ def test_fixed_dt_time_accumulates_like_reference(oracle_mod):
         t = t + 0.04
         k += 1
     assert n == k and o.state()["t"] == t
+
+
+def test_nan_depth_gives_nan_faces_in_the_oracle(oracle_mod):
+    """The reference's arithmetic propagates a NaN depth into its faces (the
+    GPU watchdog reports exactly this case)."""
+    z = np.zeros((30, 40))
+    h0 = np.full((30, 40), 0.5)
+    h0[15, 20] = np.nan
+    o = oracle_mod.Oracle(30, 40, 1.0, 1.0, z, dt_mode=0, dt=0.01)
+    o.set_state(h0)
+    o.advance(1, 1e9)
+    st = o.state()
+    assert np.isnan(st["um"]).any() or np.isnan(st["vn"]).any()
