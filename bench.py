@@ -215,6 +215,7 @@ def run_ours(args):
     peak, peak_kind = peaks()
     achieved = B_ALG_F32 * active / per_launch / 1e9
     tpc = traffic_per_cell_update()
+    kernel_desc = g.describe()
     bud = g.budget()
     vol_err = abs(bud["volume"] - (bud["volume0"] + bud["rain_in"] + bud["source_in"] - bud["evap_out"] -
                                    bud["outflow"] + bud["clamp_gain"])) / max(bud["volume"], 1e-30)
@@ -272,7 +273,7 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": (tpc * active if tpc is not None else None),
-                         "bytes_alg_per_cell_update": B_ALG_F32, "kernel": "stream_step_kernel<4,4>",
+                         "bytes_alg_per_cell_update": B_ALG_F32, "kernel": kernel_desc,
                          "launch_s": per_launch},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / k_e2e,

@@ -205,6 +205,12 @@ int sw2d_get_stream(sw2d_handle *h, void **stream);
  * launches that found the run already finished and did no work). */
 int sw2d_launch_count(sw2d_handle *h, int64_t *launches);
 
+/* One line naming the step kernel build and the decomposition the handle
+ * runs, e.g. "stream_step_kernel<8,2,1> strip_h=71 units=2378 ctas=298"
+ * (written NUL-terminated, truncated to `n` bytes).  No reference
+ * counterpart: the reference's launch shape is fixed at cu:1222-1235. */
+int sw2d_describe(const sw2d_handle *h, char *buf, int32_t n);
+
 const char *sw2d_last_error(const sw2d_handle *h);
 const char *sw2d_status_string(int32_t status);
 

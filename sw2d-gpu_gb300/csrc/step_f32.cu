@@ -25,14 +25,16 @@ cudaError_t launch_step(int th, int tw, int nblocks, const GridDesc &G, const Fo
 
 int stream_out_cols() { return kStreamOut; }
 
-// Builds of the streaming kernel the autotuner chooses from:
-// (warps per CTA, minimum resident CTAs per SM, which sets the register budget).
-#define SW2D_STREAM_VARIANTS(X) X(0, 4, 4) X(1, 4, 1) X(2, 4, 5) X(3, 4, 6) X(4, 8, 2) X(5, 2, 8)
+// Builds of the streaming kernel the autotuner chooses from: (id, warps per
+// CTA, minimum resident CTAs per SM -- which sets the register budget --,
+// unrolling of the row loop).
+#define SW2D_STREAM_VARIANTS(X) \
+    X(0, 8, 2, 1) X(1, 4, 4, 1) X(2, 8, 2, 2) X(3, 4, 4, 2) X(4, 2, 8, 1) X(5, 16, 1, 1)
 
 int stream_variants() { return 6; }
 
 int stream_warps(int variant) {
-#define SW2D_W(id, nw, mb) \
+#define SW2D_W(id, nw, mb, un) \
     if (variant == id) return nw;
     SW2D_STREAM_VARIANTS(SW2D_W)
 #undef SW2D_W
@@ -40,13 +42,33 @@ int stream_warps(int variant) {
 }
 
 cudaError_t prepare_stream_step(int variant) {
-#define SW2D_P(id, nw, mb)                                                                                   \
+#define SW2D_P(id, nw, mb, un)                                                                                 \
     if (variant == id)                                                                                      \
-        return cudaFuncSetAttribute(stream_step_kernel<nw, mb>, cudaFuncAttributePreferredSharedMemoryCarveout, \
+        return cudaFuncSetAttribute(stream_step_kernel<nw, mb, un>, cudaFuncAttributePreferredSharedMemoryCarveout, \
                                     (int)cudaSharedmemCarveoutMaxL1);
     SW2D_STREAM_VARIANTS(SW2D_P)
 #undef SW2D_P
     return cudaErrorInvalidValue;
+}
+
+const char *stream_variant_name(int variant) {
+#define SW2D_N(id, nw, mb, un) \
+    if (variant == id) return "stream_step_kernel<" #nw "," #mb "," #un ">";
+    SW2D_STREAM_VARIANTS(SW2D_N)
+#undef SW2D_N
+    return "stream_step_kernel<?>";
+}
+
+int stream_ctas_per_sm(int variant) {
+    int n = 0;
+#define SW2D_O(id, nw, mb, un)                                                                           \
+    if (variant == id &&                                                                                 \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stream_step_kernel<nw, mb, un>, nw * 32, 0) != \
+            cudaSuccess)                                                                                 \
+        n = 0;
+    SW2D_STREAM_VARIANTS(SW2D_O)
+#undef SW2D_O
+    return n;
 }
 
 cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_h, int units, const GridDesc &G,
@@ -57,9 +79,9 @@ cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_
     sh.strip_h = strip_h;
     sh.units = units;
     sh.pad = 0;
-#define SW2D_L(id, nw, mb)                                                                       \
+#define SW2D_L(id, nw, mb, un)                                                                     \
     if (variant == id) {                                                                         \
-        stream_step_kernel<nw, mb><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh);     \
+        stream_step_kernel<nw, mb, un><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh);     \
         return cudaGetLastError();                                                               \
     }
     SW2D_STREAM_VARIANTS(SW2D_L)

@@ -224,6 +224,26 @@ int upload_table(sw2d_handle *h, DevBuf &b, const T *src, size_t n) {
     return SW2D_OK;
 }
 
+// Strip height of the FP32 streaming kernel when the caller leaves it to the
+// library.  Units (column tile x strip) are sized so that a whole number of
+// waves of resident warps covers the grid -- a partial last wave leaves SMs
+// idle -- using the fewest waves whose strips are at most kMaxAutoStrip rows
+// (longer strips measured slower on GB300 at 4096^2 and up), and at least 16
+// rows, since each strip recomputes 7 halo rows.
+constexpr long long kMaxAutoStrip = 160;
+
+int auto_strip(int rows, int tiles_w, int variant, int device) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const int per_sm = stream_ctas_per_sm(variant);
+    const long long resident = (long long)(sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1) * stream_warps(variant);
+    const long long k1 = resident / (tiles_w > 0 ? tiles_w : 1);  // strips per column tile in one wave
+    if (k1 < 1) return 64;
+    long long sh = (rows + k1 - 1) / k1;
+    for (long long w = 2; sh > kMaxAutoStrip; w++) sh = (rows + w * k1 - 1) / (w * k1);
+    return (int)(sh < 16 ? 16 : sh);
+}
+
 }  // namespace
 
 namespace sw2d {
@@ -338,18 +358,7 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
         const int oc = stream_out_cols();
         h->stream_tiles_w = (cfg->cols + oc - 1) / oc;
         int sh = cfg->strip_h;
-        if (sh <= 0) {  // tallest strip that still fills the GPU with about one wave of warps
-            int dev_sms = 0;
-            cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, cfg->device);
-            const long long want = (long long)(dev_sms > 0 ? dev_sms : 152) * 20;
-            const int cand[] = {128, 96, 64, 48, 32, 24, 16};
-            sh = 16;
-            for (int c : cand)
-                if ((long long)h->stream_tiles_w * ((cfg->rows + c - 1) / c) >= want) {
-                    sh = c;
-                    break;
-                }
-        }
+        if (sh <= 0) sh = auto_strip(cfg->rows, h->stream_tiles_w, h->variant, cfg->device);
         h->strip_h = sh;
         h->stream_units = h->stream_tiles_w * ((cfg->rows + sh - 1) / sh);
         const int nw = stream_warps(h->variant);
@@ -822,6 +831,17 @@ int sw2d_get_stream(sw2d_handle *h, void **stream) {
 int sw2d_launch_count(sw2d_handle *h, int64_t *launches) {
     if (!h || !launches) return SW2D_ERR_INVALID_ARG;
     *launches = h->launches;
+    return SW2D_OK;
+}
+
+int sw2d_describe(const sw2d_handle *h, char *buf, int32_t n) {
+    if (!h || !buf || n <= 0) return SW2D_ERR_INVALID_ARG;
+    if (h->stream_kernel)
+        snprintf(buf, (size_t)n, "%s strip_h=%d units=%d ctas=%d", stream_variant_name(h->variant), h->strip_h,
+                 h->stream_units, h->nblocks);
+    else
+        snprintf(buf, (size_t)n, "step_kernel<%s,%d,%d> ctas=%d", is_f64(h) ? "double" : "float", h->tile_h,
+                 h->tile_w, h->nblocks);
     return SW2D_OK;
 }
 

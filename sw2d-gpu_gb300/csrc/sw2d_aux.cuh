@@ -42,7 +42,12 @@ __global__ void pack_depth_kernel(const double *__restrict__ src, int rows, int 
          k += (long long)gridDim.x * blockDim.x) {
         const int i = (int)(k / cols), j = (int)(k - (k / cols) * cols);
         const size_t gp = (size_t)i * pitch + j;
-        dst[gp] = mask[gp] ? (Real)src[k] : Real(0);
+        const Real v = mask[gp] ? (Real)src[k] : Real(0);
+        dst[gp] = v;
+        // the frame row below the last cell row holds a copy of its depth (the
+        // streaming kernel's face depth at the south face); the tile kernel
+        // and every other reader stop at row rows-1
+        if (i == rows - 1) dst[gp + pitch] = v;
     }
 }
 

@@ -24,8 +24,8 @@ using namespace sw2d;
 
 namespace {
 
-constexpr int kBatchWarps = 4;
-constexpr int kBatchMinBlocks = 4;
+constexpr int kBatchWarps = 8;  // the streaming kernel's default build (8 warps, 2 CTAs per SM)
+constexpr int kBatchMinBlocks = 2;
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 

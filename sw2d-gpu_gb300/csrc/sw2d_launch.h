@@ -53,6 +53,8 @@ SW2D_DECLARE_LAUNCHERS(float)
 int stream_out_cols();
 int stream_variants();
 int stream_warps(int variant);
+int stream_ctas_per_sm(int variant);
+const char *stream_variant_name(int variant);  // "stream_step_kernel<warps,minB,unroll>"  // resident CTAs per SM (occupancy), 0 on error
 cudaError_t prepare_stream_step(int variant);
 cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_h, int units, const GridDesc &G,
                                const ForcingDesc &F, const StateBufs<float> &S, const Thr<float> &T, Clock *clk,

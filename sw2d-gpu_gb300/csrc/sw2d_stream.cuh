@@ -35,7 +35,7 @@ struct StreamShape {
     int pad;
 };
 
-template <int NWARP, int MINB>
+template <int NWARP, int MINB, int UNR>
 __global__ void __launch_bounds__(NWARP * 32, MINB)
     stream_step_kernel(const GridDesc G, const ForcingDesc F, const StateBufs<float> S, const Thr<float> T,
                        Clock *__restrict__ clk, const Control *__restrict__ ctl, const int slot,
@@ -86,8 +86,8 @@ __global__ void __launch_bounds__(NWARP * 32, MINB)
         V.t1 = ci.plan.t1;
         V.dx = G.dx;
         V.dy = G.dy;
-        stream_unit(V, unit % SH.tiles_w, unit / SH.tiles_w, SH.strip_h, lane, s_sr[wid], s_sc[wid], s_q0[wid],
-                    s_q1[wid], A);
+        stream_unit<UNR>(V, unit % SH.tiles_w, unit / SH.tiles_w, SH.strip_h, lane, s_sr[wid], s_sc[wid],
+                             s_q0[wid], s_q1[wid], A);
     }
 
     // ---- warp, then CTA reductions; one thread accumulates and finishes ----

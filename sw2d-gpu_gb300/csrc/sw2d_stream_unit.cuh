@@ -43,7 +43,18 @@ struct StreamAcc {
 
 // Advances column tile `ct`, row strip `rs` (strip height strip_h) of the
 // scenario in V.  s_sr/s_sc/s_q0/s_q1 are this warp's slots for local point
-// sources (kStreamMaxSrc each).
+// sources (kStreamMaxSrc each).  UNR is the unrolling of the row loop.
+//
+// Domain edges need no tests of their own: the zero frame around every field
+// has mask 0, so the face tests on the two cells' masks already close the
+// walls and skip everything outside the domain; wall discharges are 0, so
+// the face velocities there are 0 whatever face depth divides them; and the
+// frame row below the last cell row holds a copy of that row's depth, so the
+// plain average 0.5*(x + x) = x is the reference's face depth at the south
+// face (cu:380-381), used by the open south edge.  Two rules of the
+// reference stay explicit: no cross advection u12 on column 0 (cu:178-180)
+// and no v11 on row 0 (cu:289-291).
+template <int UNR>
 __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, const int rs, const int strip_h,
                                             const int lane, int *s_sr, int *s_sc, float *s_q0, float *s_q1,
                                             StreamAcc &A) {
@@ -69,8 +80,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     const int R0 = rs * strip_h;
     const int R1 = min(R0 + strip_h, rows);
     const bool out_col = lane >= kStreamHL && lane < kStreamHL + kStreamOut && gj < cols;
-    const bool col_cell = (unsigned)gj < (unsigned)cols;
-    const bool col_vn = (unsigned)gj <= (unsigned)cols;
+    const bool not_col0 = gj != 0;
 
     // point sources inside this warp's window, in list order (the later one
     // wins on a shared cell, as the reference's assignment, cu:545)
@@ -132,7 +142,6 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         p_vn = Vin[gp];
         gp += pitch;
     };
-    (void)col_vn;
 
     // register rings: suffix = rows back from the row being read (r)
     float h1 = 0.f, h2 = 0.f, h3 = 0.f, hL1 = 0.f;
@@ -147,7 +156,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
 
     const int r_first = R0 - 4, r_last = R1 + 3;
     load_row();
-#pragma unroll 1
+#pragma unroll UNR
     for (int r = r_first; r < r_last; r++) {
         const float h0 = p_h, z0 = p_z, n0 = p_n, um0 = p_um, vn0 = p_vn;
         mb = (mb << 1) | p_m;
@@ -158,9 +167,9 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         const float hL0 = shup(h0), zL0 = shup(z0);
         const float nL0 = raster ? shup(n0) : manning;
         // ---- row r: face velocities (cu:363-453) ----
-        const float hnf = (gj == cols) ? hL0 : ((gj == 0) ? h0 : 0.50f * (h0 + hL0));
+        const float hnf = 0.50f * (h0 + hL0);
         const float vv_0 = (hnf >= ge_th) ? vn0 / hnf : 0.0f;
-        const float hmf = (r == rows) ? h1 : ((r == 0) ? h0 : 0.50f * (h0 + h1));
+        const float hmf = 0.50f * (h0 + h1);
         const float uu_0 = (hmf >= ge_th) ? um0 / hmf : 0.0f;
         const float uuL_0 = shup(uu_0);
         const float vvR_1 = shdn(vv_1);
@@ -171,38 +180,36 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         const float vnE = shdn(vn1), vnW = shup(vn1);
         const float vvW = shup(vv_1);
         float rum_1 = 0.f;
-        if (col_cell) {
-            if (i > 0 && i < rows) {
-                const float ha = h2, hb = h1, za = z2, zb = z1;
-                if (((mb >> 2) & (mb >> 1) & 1u) && ((ha >= gt_th) || (hb >= gt_th))) {
-                    if (!dry_bed<float>(T, g, ha, za, hb, zb, rum_1)) {
-                        const float hm = 0.50f * (hb + ha);
-                        const float u13 = g * hm * dt2dx * (hb + zb - ha - za);  // cu:166
-                        const float u11uur = 0.50f * (uu_0 + uu_1);
-                        const float u11uul = 0.50f * (uu_1 + uu_2);
-                        const float u11 = dt2dx * (upwind<float>(u11uur, um0, um1) - upwind_r<float>(u11uul, um2, um1));
-                        float u12 = 0.f;  // zero on column 0 (cu:178-180)
-                        if (gj != 0) {
-                            const float u12vvu = 0.50f * (vvR_1 + vvR_2);
-                            const float u12vvd = 0.50f * (vv_1 + vv_2);
-                            u12 = dt2dy * (upwind<float>(u12vvu, umE, um1) - upwind_r<float>(u12vvd, umW, um1));
-                        }
-                        const float rn = 0.5f * (n1 + n2);
-                        float ram = 0.f;
-                        if (!(hm < gt_th) && rn != 0.f) {  // cu:194-199: zero only when hm <= th
-                            const float vva = 0.250f * (vv_1 + vvR_1 + vv_2 + vvR_2);
-                            ram = g * rn * rn * sqrtf(uu_1 * uu_1 + vva * vva) / RT<float>::pow_(hm);
-                        }
-                        rum_1 = ((1.00f - dt2 * ram * 0.50f) * um1 + (-u11 - u12 - u13)) /
-                                (1.00f + dt2 * ram * 0.50f);  // cu:203
+        {
+            const float ha = h2, hb = h1, za = z2, zb = z1;
+            if (((mb >> 2) & (mb >> 1) & 1u) && ((ha >= gt_th) || (hb >= gt_th))) {
+                if (!dry_bed<float>(T, g, ha, za, hb, zb, rum_1)) {
+                    const float hm = 0.50f * (hb + ha);
+                    const float u13 = g * hm * dt2dx * (hb + zb - ha - za);  // cu:166
+                    const float u11uur = 0.50f * (uu_0 + uu_1);
+                    const float u11uul = 0.50f * (uu_1 + uu_2);
+                    const float u11 = dt2dx * (upwind<float>(u11uur, um0, um1) - upwind_r<float>(u11uul, um2, um1));
+                    float u12 = 0.f;  // zero on column 0 (cu:178-180)
+                    if (not_col0) {
+                        const float u12vvu = 0.50f * (vvR_1 + vvR_2);
+                        const float u12vvd = 0.50f * (vv_1 + vv_2);
+                        u12 = dt2dy * (upwind<float>(u12vvu, umE, um1) - upwind_r<float>(u12vvd, umW, um1));
                     }
+                    const float rn = 0.5f * (n1 + n2);
+                    float ram = 0.f;
+                    if (!(hm < gt_th) && rn != 0.f) {  // cu:194-199: zero only when hm <= th
+                        const float vva = 0.250f * (vv_1 + vvR_1 + vv_2 + vvR_2);
+                        ram = g * rn * rn * sqrtf(uu_1 * uu_1 + vva * vva) / RT<float>::pow_(hm);
+                    }
+                    rum_1 = ((1.00f - dt2 * ram * 0.50f) * um1 + (-u11 - u12 - u13)) /
+                            (1.00f + dt2 * ram * 0.50f);  // cu:203
                 }
             } else if (i == rows && V.south_open) {  // free outfall (extension)
                 if (((mb >> 2) & 1u) && h2 >= gt_th) rum_1 = 0.5440f * h2 * sqrtf(g * h2);
             }
         }
         float rvn_1 = 0.f;
-        if ((unsigned)i < (unsigned)rows && gj > 0 && gj < cols) {
+        {
             const float ha = hL1, hb = h1, za = zL1, zb = z1;
             if (((mLb >> 1) & (mb >> 1) & 1u) && ((ha >= gt_th) || (hb >= gt_th))) {
                 if (!dry_bed<float>(T, g, ha, za, hb, zb, rvn_1)) {
@@ -270,8 +277,9 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
             Hout[gp] = hw_3;
             Uout[gp] = un;
             Vout[gp] = vw;
-            if (f == rows - 1) {
+            if (f == rows - 1) {  // south face, and the depth copy below the last row
                 Uout[gp + pitch] = us;
+                Hout[gp + pitch] = hw_3;
                 A.out += us;
             }
             if (m3) {
@@ -280,13 +288,13 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
                 A.ev += ev1;
                 if (hraw < 0.f) A.clamp -= hraw;
                 // CFL bound of the new state on the owned faces (extension)
-                if (f > 0 && m4) {
+                if (m4) {
                     const float hm = 0.50f * (hw_3 + hw_4);
                     if (hm >= ge_th) A.cm = fmaxf(A.cm, fabsf(un / hm) + sqrtf(g * hm));
                 }
                 if (f == rows - 1 && V.south_open && hw_3 >= ge_th)
                     A.cm = fmaxf(A.cm, fabsf(us / hw_3) + sqrtf(g * hw_3));
-                if (gj > 0 && mL3) {
+                if (mL3) {
                     const float hn = 0.50f * (hw_3 + hwW);
                     if (hn >= ge_th) A.cm = fmaxf(A.cm, fabsf(vw / hn) + sqrtf(g * hn));
                 }

@@ -22,6 +22,21 @@ import numpy as np
 STRIPS = (16, 24, 32, 48, 64, 96, 128)
 VARIANTS = (0, 1, 2, 3, 4, 5)
 CHUNKS = (12, 24, 48, 96)
+OUT_COLS = 25            # output columns of one streaming warp
+RESIDENT_WARPS_PER_SM = 16
+
+
+# Variant ids index the kernel builds of the library; a cache written for
+# another table of builds is not reused.
+TABLE_VERSION = "stream-v2"
+
+
+def wave_strips(rows: int, cols: int, sms: int = 152, waves=(1, 2, 3, 4)):
+    """Strip heights that cut every column tile into as many strips as fill
+    the resident warps of the GPU in `w` whole waves, for each w."""
+    tiles_w = -(-cols // OUT_COLS)
+    k1 = max(1, (sms * RESIDENT_WARPS_PER_SM) // tiles_w)
+    return sorted({max(16, -(-rows // (w * k1))) for w in waves})
 
 
 def default_cache_path() -> str:
@@ -63,6 +78,14 @@ def gpu_name(device: int = 0) -> str:
         return torch.cuda.get_device_name(device)
     except Exception:
         return "unknown-gpu"
+
+
+def _sm_count(device: int = 0) -> int:
+    try:
+        import torch
+        return torch.cuda.get_device_properties(device).multi_processor_count
+    except Exception:
+        return 152
 
 
 def search(candidates, timer: Callable[[dict], float]):
@@ -112,10 +135,11 @@ def tune(rows: int, cols: int, device: int = 0, cache: Optional[Cache] = None, i
          strips=STRIPS, variants=VARIANTS, force: bool = False) -> dict:
     """Best (strip_h, variant) for a rows x cols grid on this GPU (cached)."""
     cache = cache or Cache()
-    gpu, cls = gpu_name(device), size_class(rows, cols)
+    gpu, cls = f"{gpu_name(device)}|{TABLE_VERSION}", size_class(rows, cols)
     hit = cache.get(gpu, cls)
     if hit and not force:
         return hit
+    strips = sorted(set(strips) | set(wave_strips(rows, cols, _sm_count(device))))
     cands = [{"strip_h": sh, "variant": v} for v in variants for sh in strips if sh <= max(rows, 16)]
     best, table = search(cands, _kernel_timer(rows, cols, device, iters))
     entry = {**best, "rows": rows, "cols": cols, "timings": table}
@@ -128,7 +152,7 @@ def apply(cfg, cache: Optional[Cache] = None, device: int = 0):
     import sw2d
     if cfg.precision != sw2d.PREC_F32:
         return cfg
-    hit = (cache or Cache()).get(gpu_name(device), size_class(cfg.rows, cfg.cols))
+    hit = (cache or Cache()).get(f"{gpu_name(device)}|{TABLE_VERSION}", size_class(cfg.rows, cfg.cols))
     if hit:
         cfg.strip_h = int(hit["strip_h"])
         cfg.variant = int(hit["variant"])

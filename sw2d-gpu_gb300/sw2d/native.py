@@ -82,6 +82,7 @@ _SIGS = {
     "sw2d_synchronize": (C.c_int, [C.c_void_p]),
     "sw2d_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "sw2d_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "sw2d_describe": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int32]),
     "sw2d_last_error": (C.c_char_p, [C.c_void_p]),
     "sw2d_status_string": (C.c_char_p, [C.c_int32]),
     "sw2d_volume_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_double,
@@ -246,6 +247,12 @@ class Solver:
         n = C.c_int64()
         self._check(load().sw2d_launch_count(self._h, C.byref(n)), "sw2d_launch_count")
         return int(n.value)
+
+    def describe(self) -> str:
+        """The step kernel build and decomposition this solver runs."""
+        buf = C.create_string_buffer(256)
+        self._check(load().sw2d_describe(self._h, buf, 256), "sw2d_describe")
+        return buf.value.decode()
 
     # -- outputs --------------------------------------------------------
     def field(self, which):

@@ -49,7 +49,7 @@ def main():
     g.synchronize()
     el = time.perf_counter() - t0
     print(f"precision={a.precision} size={n} kernel={a.kernel} iters={done} {el / max(done, 1) * 1e6:.1f} us/iter "
-          f"{n * n * done / el:.3e} cell-updates/s (host timed)")
+          f"{n * n * done / el:.3e} cell-updates/s (host timed); {g.describe()}")
 
 
 if __name__ == "__main__":
