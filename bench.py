@@ -160,7 +160,8 @@ def run_ours(args):
     dev = local
     torch.cuda.set_device(dev)
     sw2d.load()
-    s = scenario(SEED + rank)
+    from sw2d import replicas
+    s = scenario(replicas.rank_seed(SEED, rank))
     active = int(np.count_nonzero(s["z"] != -9999.0))
 
     g = make_solver(sw2d, s, sw2d.PREC_F32, dev)
@@ -204,14 +205,10 @@ def run_ours(args):
     clocks = sampler.stop()
     torch.cuda.synchronize()
     launches = g.launch_count() - launches0 - args.warmup * CHUNK
-    tot = sum(times)
-    if ws > 1:
-        t = torch.tensor([tot], dtype=torch.float64, device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        tot = float(t.item())
-    cu = active * CHUNK * args.steps
-    value = cu * ws / tot
-    per_launch = tot / (CHUNK * args.steps)
+    local_s = sum(times)
+    cu_all, tot = replicas.job_totals(active * CHUNK * args.steps, local_s, device=f"cuda:{dev}")
+    value = cu_all / tot  # units of all ranks / seconds of the slowest rank
+    per_launch = local_s / (CHUNK * args.steps)
     peak, peak_kind = peaks()
     achieved = B_ALG_F32 * active / per_launch / 1e9
     tpc = traffic_per_cell_update()
@@ -254,7 +251,7 @@ def run_ours(args):
     assert np.isfinite(out_h).all()
 
     # ---- batched ensemble and served stream (extra keys) --------------------
-    batched = run_batched(sw2d, dev, args) if args.batched else None
+    batched = run_batched(sw2d, dev, args, rank, ws) if args.batched else None
     served = run_served(sw2d, dev, args) if args.served else None
 
     # ---- CPU baseline: the oracle on a bounded sample ------------------------
@@ -308,15 +305,18 @@ def scen_cfg(sw2d, side, precision=None, device=0):
                                dt_mode=sw2d.DT_CFL, dt=DT_MAX, cfl=0.5, south_open=1, device=device)
 
 
-def run_batched(sw2d, dev, args):
+def run_batched(sw2d, dev, args, rank=0, ws=1):
     """The batched-ensemble configuration: 256 scenarios, sides uniform over
     {128, 256, 512, 1024}, triangular hyetographs, Manning scaling, horizon =
     rain duration + 1800 s; all advanced together until the last one ends.
     The serial FP64 plain path is timed on one scenario per size class and
-    extrapolated with the ensemble's own iteration counts."""
+    extrapolated with the ensemble's own iteration counts.  Under torchrun
+    each rank advances its contiguous share of the ensemble."""
     import torch
+    from sw2d import replicas
     from sw2d import scenarios as S
-    ens = S.ensemble(terrain_bank(), count=args.batch_count, seed=SEED + 11)
+    ens_all = S.ensemble(terrain_bank(), count=args.batch_count, seed=SEED + 11)
+    ens = [ens_all[k] for k in replicas.shard(len(ens_all), rank, ws)]
     t0 = time.perf_counter()
     b = sw2d.Batch(device=dev, chunk=24, max_scenarios=len(ens) + 8)
     ids = [b.add(scen_cfg(sw2d, e["side"], device=dev), e["z"], e["h0"], manning=e["n"],
@@ -353,12 +353,16 @@ def run_batched(sw2d, dev, args):
         rate64[side] = side * side * n / (time.perf_counter() - tt)
         g.close()
     serial64_s = sum(e["side"] * e["side"] * status[i]["steps"] / rate64[e["side"]] for e, i in zip(ens, ids))
-    return {"scenarios": len(ens), "cells": int(sum(e["side"] ** 2 for e in ens)), "cell_updates": int(cu),
-            "gpu_s": gpu_s, "wall_s_incl_admission": wall, "admission_s": t_admit, "launches": int(launches),
-            "cell_updates_per_s": cu / gpu_s, "scenarios_per_hour": len(ens) / wall * 3600.0,
-            "serial_fp64_plain_s_est": serial64_s, "fp64_plain_rate_by_side": {str(k): v for k, v in rate64.items()},
-            "scenario_throughput_vs_serial_fp64": serial64_s / wall,
-            "horizon": "rain duration + 1800 s"}
+    dev_name = f"cuda:{dev}"
+    cu_all, gpu_s_all = replicas.job_totals(cu, gpu_s, device=dev_name)
+    n_all, wall_all = replicas.job_totals(len(ens), wall, device=dev_name)
+    serial_all, _ = replicas.job_totals(serial64_s, 0.0, device=dev_name)
+    return {"scenarios": int(n_all), "cells": int(sum(e["side"] ** 2 for e in ens_all)), "cell_updates": int(cu_all),
+            "gpu_s": gpu_s_all, "wall_s_incl_admission": wall_all, "admission_s": t_admit, "launches": int(launches),
+            "cell_updates_per_s": cu_all / gpu_s_all, "scenarios_per_hour": n_all / wall_all * 3600.0,
+            "serial_fp64_plain_s_est": serial_all, "fp64_plain_rate_by_side": {str(k): v for k, v in rate64.items()},
+            "scenario_throughput_vs_serial_fp64": serial_all / wall_all,
+            "horizon": "rain duration + 1800 s", "ranks": ws}
 
 
 def run_served(sw2d, dev, args):
