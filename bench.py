@@ -253,6 +253,12 @@ def run_ours(args):
     # ---- batched ensemble and served stream (extra keys) --------------------
     batched = run_batched(sw2d, dev, args, rank, ws) if args.batched else None
     served = run_served(sw2d, dev, args) if args.served else None
+    served_sweep = None
+    if args.serve_sweep:
+        served_sweep = []
+        for rate in (float(x) for x in args.serve_sweep.split(",")):
+            args.serve_rate = rate
+            served_sweep.append(run_served(sw2d, dev, args))
 
     # ---- CPU baseline: the oracle on a bounded sample ------------------------
     cpu = cpu_sample(s, spun, budget_s=args.cpu_seconds) if rank == 0 else None
@@ -283,6 +289,8 @@ def run_ours(args):
             "batched": batched,
             "served": served,
         }
+        if served_sweep is not None:
+            line["served_sweep"] = served_sweep
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -449,6 +457,7 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=10.0)
     ap.add_argument("--serve-count", type=int, default=100)
     ap.add_argument("--serve-gb", type=float, default=40.0)
+    ap.add_argument("--serve-sweep", default="", help="comma-separated arrival rates, e.g. 2,5,10,20,50")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
