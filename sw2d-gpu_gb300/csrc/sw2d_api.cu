@@ -237,10 +237,13 @@ int auto_strip(int rows, int tiles_w, int variant, int device) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const int per_sm = stream_ctas_per_sm(variant);
     const long long resident = (long long)(sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1) * stream_warps(variant);
-    const long long k1 = resident / (tiles_w > 0 ? tiles_w : 1);  // strips per column tile in one wave
-    if (k1 < 1) return 64;
-    long long sh = (rows + k1 - 1) / k1;
-    for (long long w = 2; sh > kMaxAutoStrip; w++) sh = (rows + w * k1 - 1) / (w * k1);
+    const long long tw = tiles_w > 0 ? tiles_w : 1;
+    if (resident < tw) return 64;
+    long long sh = rows;
+    for (long long w = 1; w == 1 || sh > kMaxAutoStrip; w++) {
+        const long long k = w * resident / tw;  // strips per column tile that fill w waves
+        sh = (rows + k - 1) / k;
+    }
     return (int)(sh < 16 ? 16 : sh);
 }
 

@@ -19,6 +19,14 @@ constexpr int kStreamMaxSrc = 16;                       // point sources per war
 __device__ __forceinline__ float shup(float v) { return __shfl_up_sync(0xffffffffu, v, 1); }
 __device__ __forceinline__ float shdn(float v) { return __shfl_down_sync(0xffffffffu, v, 1); }
 
+// Upwinded flux through one side of a control volume.  The reference writes
+// it as vel*(o+s)/2 + |vel|*(s-o)/2 (cu:174, and its mirror cu:175) with vel
+// an average of two face velocities; that equals vel * (vel >= 0 ? s : o),
+// which the FP32 path evaluates with one select.  Here `vel2` is the sum of
+// the two face velocities: the halves are folded into dt2/dx and dt2/dy.
+__device__ __forceinline__ float upw(float vel2, float o, float s) { return vel2 * (vel2 >= 0.f ? s : o); }
+__device__ __forceinline__ float upw_r(float vel2, float o, float s) { return vel2 * (vel2 >= 0.f ? o : s); }
+
 // Everything a warp reads to advance one strip of one scenario.
 struct StreamView {
     int rows, cols, pitch, south_open;
@@ -60,10 +68,23 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
                                             StreamAcc &A) {
     const int rows = V.rows, cols = V.cols, pitch = V.pitch;
     const float dt2 = V.LS.dt2, dt2dx = V.LS.dt2dx, dt2dy = V.LS.dt2dy;
+    const float hdx = 0.5f * dt2dx, hdy = 0.5f * dt2dy;  // dt2/dx, dt2/dy times the halves of upw()
     const float dx = V.GS.dx, dy = V.GS.dy, g = V.GS.g, manning = V.GS.manning, rdx = V.GS.rdx, rdy = V.GS.rdy;
     const float pct_hi = V.GS.pct_hi, pct_lo = V.GS.pct_lo;
     const Thr<float> T = V.T;
     const float gt_th = T.gt_th, ge_th = T.ge_th, gt_ev = T.gt_evmin;
+    const float sqrt_g = sqrtf(g);
+    // |q/h| + sqrt(g h) with one reciprocal square root: r = 1/sqrt(h)
+    auto wave_speed = [&](float q, float h) {
+        const float r = rsqrtf(h);
+        return fabsf(q) * r * r + sqrt_g * h * r;
+    };
+    // Manning friction coefficient g n^2 |u| / h^(4/3) (cu:194-199, cu:311-316),
+    // with h^(-4/3) as 2^(-1.3333330 log2 h); zero when h <= th or n == 0
+    auto friction = [&](float rn, float speed2, float h) {
+        const float ram = g * rn * rn * sqrtf(speed2) * exp2f(-1.3333330f * __log2f(h));
+        return (!(h < gt_th) && rn != 0.f) ? ram : 0.f;
+    };
     const bool raster = V.Nin != nullptr;
     const float *__restrict__ Hin = V.Hin;
     const float *__restrict__ Uin = V.Uin;
@@ -186,21 +207,11 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
                 if (!dry_bed<float>(T, g, ha, za, hb, zb, rum_1)) {
                     const float hm = 0.50f * (hb + ha);
                     const float u13 = g * hm * dt2dx * (hb + zb - ha - za);  // cu:166
-                    const float u11uur = 0.50f * (uu_0 + uu_1);
-                    const float u11uul = 0.50f * (uu_1 + uu_2);
-                    const float u11 = dt2dx * (upwind<float>(u11uur, um0, um1) - upwind_r<float>(u11uul, um2, um1));
-                    float u12 = 0.f;  // zero on column 0 (cu:178-180)
-                    if (not_col0) {
-                        const float u12vvu = 0.50f * (vvR_1 + vvR_2);
-                        const float u12vvd = 0.50f * (vv_1 + vv_2);
-                        u12 = dt2dy * (upwind<float>(u12vvu, umE, um1) - upwind_r<float>(u12vvd, umW, um1));
-                    }
-                    const float rn = 0.5f * (n1 + n2);
-                    float ram = 0.f;
-                    if (!(hm < gt_th) && rn != 0.f) {  // cu:194-199: zero only when hm <= th
-                        const float vva = 0.250f * (vv_1 + vvR_1 + vv_2 + vvR_2);
-                        ram = g * rn * rn * sqrtf(uu_1 * uu_1 + vva * vva) / RT<float>::pow_(hm);
-                    }
+                    const float u11 = hdx * (upw(uu_0 + uu_1, um0, um1) - upw_r(uu_1 + uu_2, um2, um1));
+                    const float u12c = hdy * (upw(vvR_1 + vvR_2, umE, um1) - upw_r(vv_1 + vv_2, umW, um1));
+                    const float u12 = not_col0 ? u12c : 0.f;  // zero on column 0 (cu:178-180)
+                    const float vva = 0.250f * (vv_1 + vvR_1 + vv_2 + vvR_2);
+                    const float ram = friction(0.5f * (n1 + n2), uu_1 * uu_1 + vva * vva, hm);
                     rum_1 = ((1.00f - dt2 * ram * 0.50f) * um1 + (-u11 - u12 - u13)) /
                             (1.00f + dt2 * ram * 0.50f);  // cu:203
                 }
@@ -215,21 +226,11 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
                 if (!dry_bed<float>(T, g, ha, za, hb, zb, rvn_1)) {
                     const float hn = 0.50f * (hb + ha);
                     const float v13 = g * hn * dt2dy * (hb + zb - ha - za);  // cu:283
-                    float v11 = 0.f;                                         // zero on row 0 (cu:289-291)
-                    if (i != 0) {
-                        const float v11uur = 0.50f * (uu_0 + uuL_0);
-                        const float v11uul = 0.50f * (uu_1 + uuL_1);
-                        v11 = dt2dx * (upwind<float>(v11uur, vn0, vn1) - upwind_r<float>(v11uul, vn2, vn1));
-                    }
-                    const float v12vvu = 0.50f * (vvR_1 + vv_1);
-                    const float v12vvd = 0.50f * (vv_1 + vvW);
-                    const float v12 = dt2dy * (upwind<float>(v12vvu, vnE, vn1) - upwind_r<float>(v12vvd, vnW, vn1));
-                    const float rn = 0.5f * (n1 + nL1);
-                    float ram = 0.f;
-                    if (!(hn < gt_th) && rn != 0.f) {  // cu:311-316: zero only when hn <= th
-                        const float uua = 0.250f * (uu_1 + uu_0 + uuL_1 + uuL_0);
-                        ram = g * rn * rn * sqrtf(uua * uua + vv_1 * vv_1) / RT<float>::pow_(hn);
-                    }
+                    const float v11c = hdx * (upw(uu_0 + uuL_0, vn0, vn1) - upw_r(uu_1 + uuL_1, vn2, vn1));
+                    const float v11 = (i != 0) ? v11c : 0.f;  // zero on row 0 (cu:289-291)
+                    const float v12 = hdy * (upw(vvR_1 + vv_1, vnE, vn1) - upw_r(vv_1 + vvW, vnW, vn1));
+                    const float uua = 0.250f * (uu_1 + uu_0 + uuL_1 + uuL_0);
+                    const float ram = friction(0.5f * (n1 + nL1), uua * uua + vv_1 * vv_1, hn);
                     rvn_1 = ((1.00f - dt2 * ram * 0.50f) * vn1 + (-v11 - v12 - v13)) /
                             (1.00f + dt2 * ram * 0.50f);  // cu:320
                 }
@@ -290,13 +291,13 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
                 // CFL bound of the new state on the owned faces (extension)
                 if (m4) {
                     const float hm = 0.50f * (hw_3 + hw_4);
-                    if (hm >= ge_th) A.cm = fmaxf(A.cm, fabsf(un / hm) + sqrtf(g * hm));
+                    if (hm >= ge_th) A.cm = fmaxf(A.cm, wave_speed(un, hm));
                 }
                 if (f == rows - 1 && V.south_open && hw_3 >= ge_th)
-                    A.cm = fmaxf(A.cm, fabsf(us / hw_3) + sqrtf(g * hw_3));
+                    A.cm = fmaxf(A.cm, wave_speed(us, hw_3));
                 if (mL3) {
                     const float hn = 0.50f * (hw_3 + hwW);
-                    if (hn >= ge_th) A.cm = fmaxf(A.cm, fabsf(vw / hn) + sqrtf(g * hn));
+                    if (hn >= ge_th) A.cm = fmaxf(A.cm, wave_speed(vw, hn));
                 }
             }
             if (!isfinite(hw_3) || !isfinite(un) || !isfinite(vw)) A.bad = true;

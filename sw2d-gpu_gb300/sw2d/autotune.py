@@ -35,8 +35,7 @@ def wave_strips(rows: int, cols: int, sms: int = 152, waves=(1, 2, 3, 4)):
     """Strip heights that cut every column tile into as many strips as fill
     the resident warps of the GPU in `w` whole waves, for each w."""
     tiles_w = -(-cols // OUT_COLS)
-    k1 = max(1, (sms * RESIDENT_WARPS_PER_SM) // tiles_w)
-    return sorted({max(16, -(-rows // (w * k1))) for w in waves})
+    return sorted({max(16, -(-rows // max(1, (w * sms * RESIDENT_WARPS_PER_SM) // tiles_w))) for w in waves})
 
 
 def default_cache_path() -> str:
