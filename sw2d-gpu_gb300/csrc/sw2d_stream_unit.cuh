@@ -172,8 +172,9 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     float uu_1 = 0.f, uu_2 = 0.f, uuL_1 = 0.f;
     float vv_1 = 0.f, vv_2 = 0.f, vvR_2 = 0.f;
     float rum_2 = 0.f, rum_3 = 0.f, rvn_2 = 0.f, rvn_3 = 0.f;
-    float hs_3 = 0.f, hs_4 = 0.f, hw_4 = 0.f;
+    float hw_4 = 0.f;
     unsigned mb = 0u, mLb = 0u;  // bit k: active mask of row r-k (own / west column)
+    unsigned db = 0u;            // bit k: row r-2-k is active and dry after the provisional update
 
     const int r_first = R0 - 4, r_last = R1 + 3;
     load_row();
@@ -251,14 +252,18 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         }
 
         // ---- row r-3: dry-cell fix (cu:695-725) and final depth ----
-        const float hsW_3 = shup(hs_3);
-        const bool m3 = (mb >> 3) & 1u, m4 = (mb >> 4) & 1u, m2 = (mb >> 2) & 1u, mL3 = (mLb >> 3) & 1u;
+        // dry-cell fix (cu:695-725): a cell is "dry" when active and h* < th; its
+        // flag is kept in a bit ring, so each cell's test is made once
+        db = (db << 1) | ((((mb >> 2) & 1u) && hs_2 < ge_th) ? 1u : 0u);
+        const unsigned dbW = __shfl_up_sync(0xffffffffu, db, 1);
+        const bool m3 = (mb >> 3) & 1u, m4 = (mb >> 4) & 1u, mL3 = (mLb >> 3) & 1u;
+        const bool d2 = db & 1u, d3 = (db >> 1) & 1u, d4 = (db >> 2) & 1u, dW3 = (dbW >> 1) & 1u;
         float un = rum_3;  // x-face north of the row-(r-3) cell
-        if ((un > 0.f && m4 && hs_4 < ge_th) || (un < 0.f && m3 && hs_3 < ge_th)) un = 0.f;
+        if ((un > 0.f && d4) || (un < 0.f && d3)) un = 0.f;
         float us = rum_2;  // x-face south of it
-        if ((us > 0.f && m3 && hs_3 < ge_th) || (us < 0.f && m2 && hs_2 < ge_th)) us = 0.f;
+        if ((us > 0.f && d3) || (us < 0.f && d2)) us = 0.f;
         float vw = rvn_3;  // y-face west of it
-        if ((vw > 0.f && mL3 && hsW_3 < ge_th) || (vw < 0.f && m3 && hs_3 < ge_th)) vw = 0.f;
+        if ((vw > 0.f && dW3) || (vw < 0.f && d3)) vw = 0.f;
         const float ve = shdn(vw);
         const int f = r - 3;
         float hw_3 = 0.f, hraw = 0.f, rr1 = 0.f, pct1 = 0.f, ev1 = 0.f, ql1 = 0.f;
@@ -311,7 +316,6 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         uu_2 = uu_1; uu_1 = uu_0; uuL_1 = uuL_0;
         vv_2 = vv_1; vv_1 = vv_0; vvR_2 = vvR_1;
         rum_3 = rum_2; rum_2 = rum_1; rvn_3 = rvn_2; rvn_2 = rvn_1;
-        hs_4 = hs_3; hs_3 = hs_2;
         hw_4 = hw_3;
     }
 }
