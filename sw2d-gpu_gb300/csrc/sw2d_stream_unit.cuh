@@ -42,6 +42,15 @@ struct StreamView {
     double t0, t1, dx, dy;     // for the source rates (FP64, once per warp)
 };
 
+// Lane 0's copy of a value, for the whole warp: a value the compiler can see
+// to be warp-uniform lives in a uniform register instead of one per thread.
+__device__ __forceinline__ int wuni(int v) { return __shfl_sync(0xffffffffu, v, 0); }
+__device__ __forceinline__ float wuni(float v) { return __shfl_sync(0xffffffffu, v, 0); }
+template <class T>
+__device__ __forceinline__ T *wuni(T *p) {
+    return reinterpret_cast<T *>(__shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(p), 0));
+}
+
 // Per-warp results of a strip (per lane until reduced).
 struct StreamAcc {
     float rain, src, ev, out, clamp, cm;
@@ -66,13 +75,21 @@ template <int UNR>
 __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, const int rs, const int strip_h,
                                             const int lane, int *s_sr, int *s_sc, float *s_q0, float *s_q1,
                                             StreamAcc &A) {
-    const int rows = V.rows, cols = V.cols, pitch = V.pitch;
-    const float dt2 = V.LS.dt2, dt2dx = V.LS.dt2dx, dt2dy = V.LS.dt2dy;
+    const int rows = wuni(V.rows), cols = wuni(V.cols), pitch = wuni(V.pitch), south_open = wuni(V.south_open);
+    const float dt2 = wuni(V.LS.dt2), dt2dx = wuni(V.LS.dt2dx), dt2dy = wuni(V.LS.dt2dy);
+    const float u_ev0 = wuni(V.LS.ev0), u_ev1 = wuni(V.LS.ev1), u_rr0 = wuni(V.LS.rr0), u_rr1 = wuni(V.LS.rr1);
+    const float sx0 = wuni(V.LS.sx0), sy0 = wuni(V.LS.sy0), sx1 = wuni(V.LS.sx1), sy1 = wuni(V.LS.sy1);
+    const float storm_amp = wuni(V.GS.storm_amp), storm_2s2 = wuni(V.GS.storm_2s2);
+    const int storm = wuni((int)V.storm), on0 = wuni((int)V.on0), on1 = wuni((int)V.on1);
     const float hdx = 0.5f * dt2dx, hdy = 0.5f * dt2dy;  // dt2/dx, dt2/dy times the halves of upw()
-    const float dx = V.GS.dx, dy = V.GS.dy, g = V.GS.g, manning = V.GS.manning, rdx = V.GS.rdx, rdy = V.GS.rdy;
-    const float pct_hi = V.GS.pct_hi, pct_lo = V.GS.pct_lo;
-    const Thr<float> T = V.T;
-    const float gt_th = T.gt_th, ge_th = T.ge_th, gt_ev = T.gt_evmin;
+    const float dx = wuni(V.GS.dx), dy = wuni(V.GS.dy), g = wuni(V.GS.g), manning = wuni(V.GS.manning);
+    const float rdx = wuni(V.GS.rdx), rdy = wuni(V.GS.rdy);
+    const float pct_hi = wuni(V.GS.pct_hi), pct_lo = wuni(V.GS.pct_lo);
+    const float gt_th = wuni(V.T.gt_th), ge_th = wuni(V.T.ge_th), gt_ev = wuni(V.T.gt_evmin);
+    Thr<float> T;
+    T.gt_th = gt_th;
+    T.ge_th = ge_th;
+    T.gt_evmin = gt_ev;
     const float sqrt_g = sqrtf(g);
     // |q/h| + sqrt(g h) with one reciprocal square root: r = 1/sqrt(h)
     auto wave_speed = [&](float q, float h) {
@@ -86,15 +103,15 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         return (!(h < gt_th) && rn != 0.f) ? ram : 0.f;
     };
     const bool raster = V.Nin != nullptr;
-    const float *__restrict__ Hin = V.Hin;
-    const float *__restrict__ Uin = V.Uin;
-    const float *__restrict__ Vin = V.Vin;
-    const float *__restrict__ Zin = V.Zin;
-    const float *__restrict__ Nin = V.Nin;
-    const uint8_t *__restrict__ Min = V.Min;
-    float *__restrict__ Hout = V.Hout;
-    float *__restrict__ Uout = V.Uout;
-    float *__restrict__ Vout = V.Vout;
+    const float *__restrict__ Hin = wuni(V.Hin);
+    const float *__restrict__ Uin = wuni(V.Uin);
+    const float *__restrict__ Vin = wuni(V.Vin);
+    const float *__restrict__ Zin = wuni(V.Zin);
+    const float *__restrict__ Nin = wuni(V.Nin);
+    const uint8_t *__restrict__ Min = wuni(V.Min);
+    float *__restrict__ Hout = wuni(V.Hout);
+    float *__restrict__ Uout = wuni(V.Uout);
+    float *__restrict__ Vout = wuni(V.Vout);
 
     const int gj0 = ct * kStreamOut - kStreamHL;
     const int gj = gj0 + lane;
@@ -145,7 +162,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         if (!on) return 0.f;
         const float x = ((float)gj + 0.5f) * dx - sx;
         const float y = ((float)row + 0.5f) * dy - sy;
-        return V.GS.storm_amp * __expf(-(x * x + y * y) / V.GS.storm_2s2);
+        return storm_amp * __expf(-(x * x + y * y) / storm_2s2);
     };
 
     // row loads: rows R0-4 .. R1+2 and columns gj0 .. gj0+31 all lie inside
@@ -216,7 +233,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
                     rum_1 = ((1.00f - dt2 * ram * 0.50f) * um1 + (-u11 - u12 - u13)) /
                             (1.00f + dt2 * ram * 0.50f);  // cu:203
                 }
-            } else if (i == rows && V.south_open) {  // free outfall (extension)
+            } else if (i == rows && south_open) {  // free outfall (extension)
                 if (((mb >> 2) & 1u) && h2 >= gt_th) rum_1 = 0.5440f * h2 * sqrtf(g * h2);
             }
         }
@@ -245,9 +262,9 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
             const float ho = h2;
             const bool hi = ho >= gt_ev;
             const float pct = hi ? pct_hi : pct_lo;
-            const float evapo = hi ? V.LS.ev0 : 0.f;
+            const float evapo = hi ? u_ev0 : 0.f;
             const float ql = nsrc ? source_at(r - 2, false) : 0.f;
-            const float rr = V.storm ? storm_rate(r - 2, V.on0, V.LS.sx0, V.LS.sy0) : V.LS.rr0;
+            const float rr = storm ? storm_rate(r - 2, on0, sx0, sy0) : u_rr0;
             hs_2 = fmaxf(ho - dt2 * ((rum_1 - rum_2) * rdx + (rvnE_2 - rvn_2) * rdy - ql - rr * pct + evapo), 0.f);
         }
 
@@ -271,9 +288,9 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
             const float ho = h3;
             const bool hi = ho >= gt_ev;
             pct1 = hi ? pct_hi : pct_lo;
-            ev1 = hi ? V.LS.ev1 : 0.f;
+            ev1 = hi ? u_ev1 : 0.f;
             ql1 = nsrc ? source_at(f, true) : 0.f;
-            rr1 = V.storm ? storm_rate(f, V.on1, V.LS.sx1, V.LS.sy1) : V.LS.rr1;
+            rr1 = storm ? storm_rate(f, on1, sx1, sy1) : u_rr1;
             hraw = ho - dt2 * ((us - un) * rdx + (ve - vw) * rdy - ql1 - rr1 * pct1 + ev1);
             hw_3 = fmaxf(hraw, 0.f);
         }
@@ -298,7 +315,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
                     const float hm = 0.50f * (hw_3 + hw_4);
                     if (hm >= ge_th) A.cm = fmaxf(A.cm, wave_speed(un, hm));
                 }
-                if (f == rows - 1 && V.south_open && hw_3 >= ge_th)
+                if (f == rows - 1 && south_open && hw_3 >= ge_th)
                     A.cm = fmaxf(A.cm, wave_speed(us, hw_3));
                 if (mL3) {
                     const float hn = 0.50f * (hw_3 + hwW);
