@@ -25,11 +25,18 @@ cudaError_t launch_step(int th, int tw, int nblocks, const GridDesc &G, const Fo
 
 int stream_out_cols() { return kStreamOut; }
 
+// Shared-memory share of the L1/shared split for the streaming kernel, in
+// percent.  Each CTA needs only a few KB (source slots and the reduction, plus
+// the 1 KB the system reserves), but asking for the largest L1 left room for
+// just 2-3 CTAs per SM and capped the occupancy of the smaller-CTA builds.
+constexpr int kStreamCarveoutPercent = 25;
+
 // Builds of the streaming kernel the autotuner chooses from: (id, warps per
-// CTA, minimum resident CTAs per SM -- which sets the register budget --,
-// unrolling of the row loop).
+// CTA, minimum resident CTAs per SM -- which sets the register budget: 20
+// warps per SM fit 96 registers, 16 fit 128, 24 fit 80 --, unrolling of the
+// row loop).  Build 0 is the default.
 #define SW2D_STREAM_VARIANTS(X) \
-    X(0, 8, 2, 1) X(1, 4, 4, 1) X(2, 8, 2, 2) X(3, 4, 4, 2) X(4, 2, 8, 1) X(5, 16, 1, 1)
+    X(0, 2, 10, 1) X(1, 8, 2, 1) X(2, 4, 5, 1) X(3, 12, 2, 1) X(4, 8, 2, 2) X(5, 4, 4, 1)
 
 int stream_variants() { return 6; }
 
@@ -45,7 +52,7 @@ cudaError_t prepare_stream_step(int variant) {
 #define SW2D_P(id, nw, mb, un)                                                                                 \
     if (variant == id)                                                                                      \
         return cudaFuncSetAttribute(stream_step_kernel<nw, mb, un>, cudaFuncAttributePreferredSharedMemoryCarveout, \
-                                    (int)cudaSharedmemCarveoutMaxL1);
+                                    kStreamCarveoutPercent);
     SW2D_STREAM_VARIANTS(SW2D_P)
 #undef SW2D_P
     return cudaErrorInvalidValue;

@@ -23,19 +23,20 @@ STRIPS = (16, 24, 32, 48, 64, 96, 128)
 VARIANTS = (0, 1, 2, 3, 4, 5)
 CHUNKS = (12, 24, 48, 96)
 OUT_COLS = 25            # output columns of one streaming warp
-RESIDENT_WARPS_PER_SM = 16
+RESIDENT_WARPS_PER_SM = (16, 20, 24)  # resident warps per SM of the kernel builds
 
 
 # Variant ids index the kernel builds of the library; a cache written for
 # another table of builds is not reused.
-TABLE_VERSION = "stream-v2"
+TABLE_VERSION = "stream-v3"
 
 
-def wave_strips(rows: int, cols: int, sms: int = 152, waves=(1, 2, 3, 4)):
+def wave_strips(rows: int, cols: int, sms: int = 152, waves=(1, 2, 3, 4), warps_per_sm=RESIDENT_WARPS_PER_SM):
     """Strip heights that cut every column tile into as many strips as fill
-    the resident warps of the GPU in `w` whole waves, for each w."""
+    the resident warps of the GPU in `w` whole waves, for each w and each
+    resident-warp count of the kernel builds."""
     tiles_w = -(-cols // OUT_COLS)
-    return sorted({max(16, -(-rows // max(1, (w * sms * RESIDENT_WARPS_PER_SM) // tiles_w))) for w in waves})
+    return sorted({max(16, -(-rows // max(1, (w * sms * per) // tiles_w))) for w in waves for per in warps_per_sm})
 
 
 def default_cache_path() -> str:
