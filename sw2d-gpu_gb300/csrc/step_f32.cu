@@ -36,7 +36,7 @@ constexpr int kStreamCarveoutPercent = 25;
 // warps per SM fit 96 registers, 16 fit 128, 24 fit 80 --, unrolling of the
 // row loop).  Build 0 is the default.
 #define SW2D_STREAM_VARIANTS(X) \
-    X(0, 2, 10, 1) X(1, 8, 2, 1) X(2, 4, 5, 1) X(3, 12, 2, 1) X(4, 8, 2, 2) X(5, 4, 4, 1)
+    X(0, 2, 10, 2) X(1, 2, 10, 1) X(2, 4, 5, 2) X(3, 8, 2, 1) X(4, 8, 2, 2) X(5, 12, 2, 1)
 
 int stream_variants() { return 6; }
 
