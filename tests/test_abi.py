@@ -44,7 +44,8 @@ def test_invalid_configs_rejected_before_any_gpu_call(sw2d_mod):
     L = sw2d_mod.load()
     h = C.c_void_p()
     for kw in ({"rows": 0, "cols": 4}, {"rows": 4, "cols": 4, "dx": 0.0}, {"rows": 4, "cols": 4, "dt": -1.0},
-               {"rows": 4, "cols": 4, "precision": 7}, {"rows": 4, "cols": 4, "dt_mode": 1, "cfl": 0.0}):
+               {"rows": 4, "cols": 4, "precision": 7}, {"rows": 4, "cols": 4, "dt_mode": 1, "cfl": 0.0},
+               {"rows": 60000, "cols": 60000}):  # beyond 32-bit field offsets
         c = sw2d_mod.default_config(**kw)
         assert L.sw2d_create(C.byref(c), C.byref(h)) == 1
     assert L.sw2d_create(None, C.byref(h)) == 1
@@ -62,3 +63,17 @@ def test_status_strings(sw2d_mod):
     L = sw2d_mod.load()
     assert L.sw2d_status_string(0) == b"ok"
     assert L.sw2d_status_string(4) == b"non-finite value produced"
+
+
+@pytest.mark.gpu
+def test_describe_names_the_kernel_run(sw2d_mod):
+    g = sw2d_mod.Solver(rows=300, cols=200, dx=1.0, dy=1.0)
+    assert g.describe().startswith("step_kernel<double,")
+    g.close()
+    g = sw2d_mod.Solver(rows=300, cols=200, dx=1.0, dy=1.0, precision=sw2d_mod.PREC_F32, dt_mode=sw2d_mod.DT_CFL)
+    d = g.describe()
+    assert d.startswith("stream_step_kernel<") and "strip_h=" in d
+    strip = int(d.split("strip_h=")[1].split()[0])
+    units = int(d.split("units=")[1].split()[0])
+    assert units == -(-200 // 25) * -(-300 // strip)  # column tiles x strips
+    g.close()
