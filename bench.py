@@ -47,6 +47,7 @@ DT_MAX = 1.0             # largest half step [s]
 B_ALG_F32 = 32           # algorithmic bytes per cell-update: read h,um,vn,z,n + write h,um,vn (FP32)
 B_ALG_F64 = 64
 METRIC = "cell-updates/s"
+ACC_WINDOW_S = 60.0      # simulated seconds of the FP32-vs-FP64 accuracy leg
 
 
 def log(*a):
@@ -225,6 +226,9 @@ def run_ours(args):
     v64 = active * CHUNK * len(t64) / sum(t64)
     g64.close()
 
+    # ---- error of the FP32 path against FP64 on this workload ---------------
+    accuracy = fp32_vs_fp64(sw2d, s, spun, dev)
+
     # ---- end to end through the C ABI with host buffers ----------------------
     k_e2e = max(3, args.steps // 4)
     h_pinned = torch.from_numpy(s["h0"]).pin_memory()
@@ -286,6 +290,7 @@ def run_ours(args):
             "wall_s_timed": wall,
             "fp64_plain": {"value": v64, "unit": "cell-updates/s", "speedup_f32_over_f64": value / ws / v64},
             "volume_rel_error": vol_err,
+            "accuracy_vs_fp64": accuracy,
             "batched": batched,
             "served": served,
         }
@@ -311,6 +316,31 @@ def scen_cfg(sw2d, side, precision=None, device=0):
     return sw2d.default_config(rows=side, cols=side, dx=DX, dy=DX,
                                precision=sw2d.PREC_F32 if precision is None else precision,
                                dt_mode=sw2d.DT_CFL, dt=DT_MAX, cfl=0.5, south_open=1, device=device)
+
+
+def depth_error(a, b, th=1.0e-4):
+    """max |dh| [m], its 99.99th percentile and the flooded-area (h > th)
+    relative difference of depth rasters a (FP64) and b."""
+    d = np.abs(a - b)
+    wa, wb = int(np.count_nonzero(a > th)), int(np.count_nonzero(b > th))
+    return {"max_abs_dh_m": float(d.max()), "p9999_abs_dh_m": float(np.percentile(d, 99.99)),
+            "flooded_area_rel_diff": abs(wa - wb) / max(wa, 1)}
+
+
+def fp32_vs_fp64(sw2d, s, spun, dev, window=ACC_WINDOW_S):
+    """FP32 and FP64 advanced from the same spun-up state to the same
+    simulated time (each with its own CFL steps); the depth error of FP32."""
+    out = {}
+    for prec in (sw2d.PREC_F64, sw2d.PREC_F32):
+        g = make_solver(sw2d, s, prec, dev)
+        g.set_state(spun["h"], spun["um"], spun["vn"], t0=SPINUP_T)
+        g.advance(10 ** 9, t_end=SPINUP_T + window)
+        out[prec] = (g.depth(), g.budget())
+        g.close()
+    e = depth_error(out[sw2d.PREC_F64][0], out[sw2d.PREC_F32][0])
+    e.update({"window_s": window, "from_t_s": SPINUP_T, "steps_fp64": int(out[sw2d.PREC_F64][1]["steps"]),
+              "steps_fp32": int(out[sw2d.PREC_F32][1]["steps"])})
+    return e
 
 
 def run_batched(sw2d, dev, args, rank=0, ws=1):
@@ -344,6 +374,21 @@ def run_batched(sw2d, dev, args, rank=0, ws=1):
     status = b.poll()
     cu = sum(e["side"] * e["side"] * status[i]["steps"] for e, i in zip(ens, ids))
     launches = b.launch_count() - launches0
+    # error against FP64: one scenario per side class up to 512, rerun alone
+    # through the FP64 plain path to the same end time
+    errors = []
+    for side in sorted({e["side"] for e in ens if e["side"] <= 512}):
+        k = next(j for j, e in enumerate(ens) if e["side"] == side)
+        e = ens[k]
+        g = sw2d.Solver(scen_cfg(sw2d, side, precision=sw2d.PREC_F64, device=dev))
+        g.set_static(e["z"], e["n"])
+        g.set_state(e["h0"])
+        g.set_rain(sw2d.RAIN_LINEAR, e["rain"], e["rain_dt"])
+        g.advance(10 ** 9, t_end=e["t_end"])
+        err = depth_error(g.depth(), b.field(ids[k], sw2d.FIELD_DEPTH))
+        err["side"] = side
+        errors.append(err)
+        g.close()
     b.close()
     # serial FP64 plain path, per size class
     rate64 = {}
@@ -370,7 +415,7 @@ def run_batched(sw2d, dev, args, rank=0, ws=1):
             "cell_updates_per_s": cu_all / gpu_s_all, "scenarios_per_hour": n_all / wall_all * 3600.0,
             "serial_fp64_plain_s_est": serial_all, "fp64_plain_rate_by_side": {str(k): v for k, v in rate64.items()},
             "scenario_throughput_vs_serial_fp64": serial_all / wall_all,
-            "horizon": "rain duration + 1800 s", "ranks": ws}
+            "horizon": "rain duration + 1800 s", "ranks": ws, "accuracy_vs_fp64": errors}
 
 
 def run_served(sw2d, dev, args):

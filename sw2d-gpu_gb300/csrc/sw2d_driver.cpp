@@ -18,9 +18,19 @@
 //   db/<case>/output/WaterLevel.txt     probe depths             (cu:1386-1410)
 //   db/<case>/output/TimeSimu_<k>.txt   run time                 (cu:1477-1485)
 //
-// Usage: sw2d_run [--db DIR] [--precision f64|f32] [--cfl C] [--max-outputs N]
+// Extensions, off unless asked for, so the reference's datasets give the
+// reference's outputs:
+//   db/<case>/input/manning.txt         per-cell Manning n, ESRI ASCII of the
+//                                       DEM's shape (used when present; the
+//                                       reference has one scalar, cu:799)
+//   db/<case>/output/Outflow.txt        outflow hydrograph of the open south
+//                                       edge (--south-open): time, cumulative
+//                                       volume, mean rate since the last line
+//
+// Usage: sw2d_run [--db DIR] [--precision f64|f32] [--cfl C] [--south-open] [--max-outputs N]
 //   --precision f64 (default) runs the reference's scheme with its fixed dt;
-//   --cfl C switches to the CFL rule; --max-outputs stops after N VTK files.
+//   --cfl C switches to the CFL rule; --south-open opens the south edge (free
+//   outfall); --max-outputs stops after N VTK files.
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -187,6 +197,7 @@ struct Opts {
     std::string db = "db";
     int precision = SW2D_PREC_F64;
     double cfl = 0.0;
+    bool south_open = false;
     long max_outputs = -1;
 };
 
@@ -252,6 +263,13 @@ int run_case(const Opts &o, const std::string &name) {
         Rg.resize(n);
         evapo = evaporation_series(T, Rg, albedo, dtrain);
     }
+    // optional roughness raster (extension)
+    Esri nman;
+    const bool has_n = file_exists(in + "manning.txt");
+    if (has_n && (!read_esri(in + "manning.txt", nman) || nman.rows != rows || nman.cols != cols)) {
+        std::printf("unknown file - manning.txt\n");
+        return 1;
+    }
     std::vector<double> ic = read_numbers(in + "initial_condition.txt");
     if (ic.size() < ncell) {
         std::printf("unknown file - initial_condition.txt\n");
@@ -296,9 +314,10 @@ int run_case(const Opts &o, const std::string &name) {
         cfg.dt_mode = SW2D_DT_CFL;
         cfg.cfl = o.cfl;
     }
+    cfg.south_open = o.south_open ? 1 : 0;
     sw2d_handle *h = nullptr;
     check(nullptr, sw2d_create(&cfg, &h), "sw2d_create");
-    check(h, sw2d_set_static(h, dem.v.data(), nullptr), "sw2d_set_static");
+    check(h, sw2d_set_static(h, dem.v.data(), has_n ? nman.v.data() : nullptr), "sw2d_set_static");
     check(h, sw2d_set_state(h, ic.data(), nullptr, nullptr, time0), "sw2d_set_state");
     check(h, sw2d_set_rain(h, SW2D_RAIN_COMPAT, rain.data(), (int32_t)rain.size(), dtrain), "sw2d_set_rain");
     if (!evapo.empty())
@@ -318,6 +337,16 @@ int run_case(const Opts &o, const std::string &name) {
         return 1;
     }
     if (su.out_outlet != 1) std::fprintf(wl, "%s\n", "Outlet off");
+    FILE *hyd = nullptr;  // outflow hydrograph (extension)
+    double hyd_t = time0, hyd_v = 0.0;
+    if (o.south_open) {
+        hyd = std::fopen((out + "Outflow.txt").c_str(), "w");
+        if (!hyd) {
+            std::printf("cannot write %sOutflow.txt\n", out.c_str());
+            return 1;
+        }
+        std::fprintf(hyd, "%s\n", "time_s outflow_volume_m3 outflow_rate_m3_per_s");
+    }
     // probe cells in the row-major order the reference visits them (cu:1388-1410)
     std::vector<long> probe_km;
     for (auto &p : probes) {
@@ -396,6 +425,14 @@ int run_case(const Opts &o, const std::string &name) {
                         std::fprintf(wl, npout == n_out ? " %lf\n" : " %lf", v);
                     }
         }
+        if (hyd) {
+            sw2d_budget b;
+            check(h, sw2d_get_budget(h, &b), "sw2d_get_budget");
+            const double rate = b.t > hyd_t ? (b.outflow - hyd_v) / (b.t - hyd_t) : 0.0;
+            std::fprintf(hyd, "%lf %.9e %.9e\n", b.t, b.outflow, rate);
+            hyd_t = b.t;
+            hyd_v = b.outflow;
+        }
         outputs++;
         first = false;
         if (o.max_outputs >= 0 && outputs >= o.max_outputs) break;
@@ -408,6 +445,7 @@ int run_case(const Opts &o, const std::string &name) {
         std::fclose(ts);
     }
     std::fclose(wl);
+    if (hyd) std::fclose(hyd);
     sw2d_destroy(h);
     return 0;
 }
@@ -423,8 +461,10 @@ int main(int argc, char **argv) {
         else if (a == "--precision") o.precision = next() == "f32" ? SW2D_PREC_F32 : SW2D_PREC_F64;
         else if (a == "--cfl") o.cfl = std::atof(next().c_str());
         else if (a == "--max-outputs") o.max_outputs = std::atol(next().c_str());
+        else if (a == "--south-open") o.south_open = true;
         else {
-            std::fprintf(stderr, "usage: %s [--db DIR] [--precision f64|f32] [--cfl C] [--max-outputs N]\n", argv[0]);
+            std::fprintf(stderr, "usage: %s [--db DIR] [--precision f64|f32] [--cfl C] [--south-open] [--max-outputs N]\n",
+                         argv[0]);
             return 2;
         }
     }

@@ -65,3 +65,37 @@ def test_driver_second_output_matches_oracle(sw2d_mod, oracle_mod, tmp_path):
     assert o.advance(750, 6000.0) == 750
     ref = np.array([float("%f" % v) for v in o.state()["h"].ravel()]).reshape(100, 100)
     assert np.array_equal(depth, ref)
+
+
+@pytest.mark.gpu
+def test_driver_roughness_raster_and_outflow_hydrograph(sw2d_mod, oracle_mod, tmp_path):
+    """Extensions: input/manning.txt (per-cell n) and --south-open with the
+    outflow hydrograph file; the 60 s depth and outflow volume against the
+    oracle run with the same raster and open edge."""
+    db = _db(tmp_path)
+    case = db / "dam_break"
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "dam_break.npz"))
+    n = 0.010 + 0.040 * np.repeat(np.arange(100)[:, None] / 99.0, 100, axis=1)
+    head = (case / "input" / "dem.txt").read_text().split("\n")[:6]
+    body = "\n".join(" ".join("%.6f" % v for v in row) for row in n)
+    (case / "input" / "manning.txt").write_text("\n".join(head) + "\n" + body + "\n")
+    n = np.array([[float("%.6f" % v) for v in row] for row in n])
+    r = subprocess.run([_driver(sw2d_mod), "--db", str(db), "--south-open", "--max-outputs", "3"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    txt = (case / "output" / "Results_1.vtk").read_text().split("\n")
+    k = txt.index("SCALARS depth float 1") + 2
+    depth = np.array([float(x) for x in txt[k:k + 10000]]).reshape(100, 100)[::-1]
+    o = oracle_mod.Oracle(100, 100, 10.0, 10.0, d["z"], n=n, manning=float(d["manning"]), INT=float(d["INT"]),
+                          INF=float(d["INF"]), LWL=float(d["LWL"]), EV_WL_min=float(d["EV_WL_min"]), dt_mode=0,
+                          dt=0.04, south_open=1)
+    o.set_state(d["h0"])
+    assert o.advance(750, 6000.0) == 750
+    ref = np.array([float("%f" % v) for v in o.state()["h"].ravel()]).reshape(100, 100)
+    assert np.array_equal(depth, ref)
+    lines = (case / "output" / "Outflow.txt").read_text().strip().split("\n")
+    assert lines[0].split() == ["time_s", "outflow_volume_m3", "outflow_rate_m3_per_s"]
+    rows = [[float(x) for x in l.split()] for l in lines[1:]]
+    assert len(rows) == 3
+    assert all(b[1] >= a[1] for a, b in zip(rows, rows[1:]))  # cumulative volume never decreases
+    assert rows[1][1] == pytest.approx(o.budget()["outflow"], rel=1e-9, abs=1e-9)
