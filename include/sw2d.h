@@ -155,6 +155,14 @@ int sw2d_set_rain(sw2d_handle *h, int32_t kind, const double *series, int32_t n,
 int sw2d_set_storm(sw2d_handle *h, double peak_mm_h, double x0, double y0, double vx,
                    double vy, double sigma, double t_stop);
 
+/* Spatial rain distribution (extension for rainfall rasters; the reference
+ * rains one interpolated value on every cell, cu:654): per-cell factors,
+ * rows*cols values north row first, finite and >= 0, that multiply the rain
+ * rate of whatever rain kind is set (series or storm), in both continuity
+ * calls and in the rain budget.  NULL restores uniform rain.  Call after
+ * sw2d_set_static, which clears the factors. */
+int sw2d_set_rain_weights(sw2d_handle *h, const double *w);
+
 /* Evaporation series in mm per interval, reference formula
  * (evaporation_load cu:589-601, d_Ev uploads cu:1284, cu:1309); applied
  * where the depth is above EV_WL_min (cu:627-634).  n = 0 disables it. */

@@ -46,6 +46,7 @@ class Forcing(C.Structure):
         ("n_src", C.c_int32), ("n_qrec", C.c_int32),
         ("src_cell", C.POINTER(C.c_int32)), ("src_q", C.POINTER(C.c_double)),
         ("dtoq", C.c_double),
+        ("rain_w", C.POINTER(C.c_double)),
     ]
 
 
@@ -101,7 +102,7 @@ class OracleForcing:
     """Holds the numpy buffers behind a ``Forcing`` struct."""
 
     def __init__(self, rain_kind=RAIN_NONE, rain=None, rain_dt=1.0, storm=None,
-                 ev=None, ev_dt=1.0, sources=None, src_q=None, dtoq=1.0):
+                 ev=None, ev_dt=1.0, sources=None, src_q=None, dtoq=1.0, rain_w=None):
         self._keep = []
         f = Forcing()
         f.rain_kind = rain_kind
@@ -132,6 +133,10 @@ class OracleForcing:
             f.src_cell = cells.ctypes.data_as(C.POINTER(C.c_int32))
             f.src_q = q.ctypes.data_as(C.POINTER(C.c_double))
         f.dtoq = dtoq
+        if rain_w is not None:
+            w = _f64(rain_w)
+            self._keep.append(w)
+            f.rain_w = w.ctypes.data_as(C.POINTER(C.c_double))
         self.struct = f
 
 

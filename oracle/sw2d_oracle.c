@@ -89,6 +89,10 @@ typedef struct {
     const int32_t *src_cell; /* linear cell index i*cols+j of each source */
     const double *src_q;  /* [n_qrec][n_src] discharges, m^3/s */
     double dtoq;
+    /* spatial rain distribution (extension; the reference rains one value
+       on every cell, cu:654): per-cell factors rows*cols applied to the rain
+       rate of the kind above, or NULL for uniform rain */
+    const double *rain_w;
 } orc_forcing;
 
 typedef struct { double s, c; } kahan;
@@ -532,6 +536,7 @@ static void continuity(const orc_params *p, const orc_forcing *f, const double *
                 evapo = 0.000;
             }
             double rr = rain_cell(f, p, t, i, j, rr_u);
+            if (f->rain_w) rr = rr * f->rain_w[(size_t)i * cols + j];
             double ql = w->ql[c];
             /* cu:654 */
             double hv = ho[c] - dt2 * ((um[XI(i + 1, j)] - um[c]) / dx + (vn[YI(i, j + 1)] - vn[YI(i, j)]) / dy - ql - rr * pct + evapo);

@@ -44,6 +44,8 @@ struct sw2d_handle {
     void *h[2] = {nullptr, nullptr}, *um[2] = {nullptr, nullptr}, *vn[2] = {nullptr, nullptr};
     void *z = nullptr, *nman = nullptr;
     uint8_t *mask = nullptr;
+    void *rainw = nullptr;  // spatial rain factors (allocated on first use)
+    bool use_rainw = false;
     double *stage = nullptr, *stage2 = nullptr;
     size_t stage_elems = 0;
     double *partial = nullptr;
@@ -123,6 +125,7 @@ StateBufs<Real> make_bufs(const sw2d_handle *h) {
     s.z = (const Real *)h->z;
     s.nman = h->has_nraster ? (const Real *)h->nman : nullptr;
     s.mask = h->mask;
+    s.rainw = h->use_rainw ? (const Real *)h->rainw : nullptr;
     return s;
 }
 
@@ -409,6 +412,7 @@ int sw2d_destroy(sw2d_handle *h) {
     free_field(h->z, h->real_size);
     free_field(h->nman, h->real_size);
     free_field(h->mask, 1);
+    free_field(h->rainw, h->real_size);
     cudaFree(h->stage);
     cudaFree(h->stage2);
     cudaFree(h->partial);
@@ -443,7 +447,38 @@ int sw2d_set_static(sw2d_handle *h, const double *z, const double *manning) {
     h->has_nraster = manning != nullptr;
     h->have_static = true;
     h->have_state = false;  // the active mask may have changed
+    h->use_rainw = false;   // rain factors were packed with the old mask
     h->graph_valid = false;
+    return SW2D_OK;
+}
+
+int sw2d_set_rain_weights(sw2d_handle *h, const double *w) {
+    if (!h) return SW2D_ERR_INVALID_ARG;
+    if (!h->have_static) return fail(h, SW2D_ERR_STATE, "sw2d_set_rain_weights needs sw2d_set_static first");
+    h->graph_valid = false;
+    if (!w) {
+        h->use_rainw = false;
+        return SW2D_OK;
+    }
+    const int rows = h->cfg.rows, cols = h->cfg.cols;
+    const size_t n = (size_t)rows * cols;
+    for (size_t k = 0; k < n; k++)
+        if (!(w[k] >= 0.0) || !std::isfinite(w[k]))
+            return fail(h, SW2D_ERR_INVALID_ARG, "rain weights must be finite and >= 0");
+    if (!h->rainw) {
+        void *p = nullptr;
+        const size_t bytes = h->plane * h->real_size;
+        CK(h, cudaMalloc(&p, bytes));
+        CK(h, cudaMemsetAsync(p, 0, bytes, h->stream));  // zero frame
+        h->rainw = static_cast<char *>(p) + h->origin * h->real_size;
+    }
+    CK(h, cudaMemcpyAsync(h->stage, w, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (is_f64(h))
+        CK(h, launch_pack_depth(h->stage, rows, cols, h->pitch, h->mask, (double *)h->rainw, h->stream));
+    else
+        CK(h, launch_pack_depth(h->stage, rows, cols, h->pitch, h->mask, (float *)h->rainw, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->use_rainw = true;
     return SW2D_OK;
 }
 

@@ -96,6 +96,7 @@ __global__ void __launch_bounds__(NWARP * 32, MINB) batch_step_kernel(const Batc
             V.Zin = S.z;
             V.Nin = S.nman;
             V.Min = S.mask;
+            V.Win = nullptr;  // batched scenarios rain uniformly
             V.Hout = S.h[1 - b];
             V.Uout = S.um[1 - b];
             V.Vout = S.vn[1 - b];
@@ -115,7 +116,7 @@ __global__ void __launch_bounds__(NWARP * 32, MINB) batch_step_kernel(const Batc
             A.rain = A.src = A.ev = A.out = A.clamp = A.cm = 0.f;
             A.bad = A.too_many_sources = false;
             const int ct = ue.y % S.tiles_w, rs = ue.y / S.tiles_w;
-            stream_unit<1>(V, ct, rs, S.strip_h, lane, s_sr[wid], s_sc[wid], s_q0[wid], s_q1[wid], A);
+            stream_unit<1, false>(V, ct, rs, S.strip_h, lane, s_sr[wid], s_sc[wid], s_q0[wid], s_q1[wid], A);
             warp_reduce_acc(A);
             if (lane == 0) {
                 const double area = S.G.dx * S.G.dy, scale = ci.plan.d.dt2 * area;

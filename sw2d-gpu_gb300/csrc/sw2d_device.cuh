@@ -144,6 +144,7 @@ struct StateBufs {
     const Real *z;
     const Real *nman;  // per-cell Manning n or nullptr
     const uint8_t *mask;
+    const Real *rainw;  // per-cell factors of the rain rate, or nullptr (uniform rain)
 };
 
 // wet/dry thresholds as `x >= c` constants (see file comment)
@@ -633,6 +634,7 @@ __global__ void __launch_bounds__(NT)
 
     const Real rr0_u = LS.rr0, rr1_u = LS.rr1;
     const Real ev0 = LS.ev0, ev1 = LS.ev1;
+    const Real *__restrict__ W = S.rainw;  // spatial rain factors (extension) or nullptr
     const int nloc = s_nloc;
     const Real pct_hi = GS.pct_hi, pct_lo = GS.pct_lo;
     const bool storm = F.rain_kind == RAIN_STORM;
@@ -777,7 +779,8 @@ __global__ void __launch_bounds__(NT)
             Real ql = 0;
             for (int q = 0; q < nloc; q++)
                 if (s_srcp[q] == p) ql = s_srcq0[q];
-            const Real rr = storm ? storm_rate(I0 + r, J0 + c, pl.storm_on0, sx0, sy0) : rr0_u;
+            Real rr = storm ? storm_rate(I0 + r, J0 + c, pl.storm_on0, sx0, sy0) : rr0_u;
+            if (W) rr = rr * W[(size_t)(I0 + r) * pitch + (J0 + c)];
             hv = ho - dt2 * ((s_rum[p + RW] - s_rum[p]) / dx + (s_rvn[p + 1] - s_rvn[p]) / dy - ql - rr * pct + evapo);
             hv = fmax(hv, Real(0.00));  // cu:657
         }
@@ -820,6 +823,7 @@ __global__ void __launch_bounds__(NT)
             for (int q = 0; q < nloc; q++)
                 if (s_srcp[q] == p) ql = s_srcq1[q];
             rr = storm ? storm_rate(gi, gj, pl.storm_on1, sx1, sy1) : rr1_u;
+            if (W) rr = rr * W[(size_t)gi * pitch + gj];
             hraw = ho - dt2 * ((us - un) / dx + (ve - vw) / dy - ql - rr * pct + evapo);
             hv = fmax(hraw, Real(0.00));
         }

@@ -35,7 +35,7 @@ struct StreamShape {
     int pad;
 };
 
-template <int NWARP, int MINB, int UNR>
+template <int NWARP, int MINB, int UNR, bool RAINW>
 __global__ void __launch_bounds__(NWARP * 32, MINB)
     stream_step_kernel(const GridDesc G, const ForcingDesc F, const StateBufs<float> S, const Thr<float> T,
                        Clock *__restrict__ clk, const Control *__restrict__ ctl, const int slot,
@@ -74,6 +74,7 @@ __global__ void __launch_bounds__(NWARP * 32, MINB)
         V.Zin = S.z;
         V.Nin = S.nman;
         V.Min = S.mask;
+        V.Win = S.rainw;
         V.Hout = S.h[1 - b];
         V.Uout = S.um[1 - b];
         V.Vout = S.vn[1 - b];
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(NWARP * 32, MINB)
         V.t1 = ci.plan.t1;
         V.dx = G.dx;
         V.dy = G.dy;
-        stream_unit<UNR>(V, unit % SH.tiles_w, unit / SH.tiles_w, SH.strip_h, lane, s_sr[wid], s_sc[wid],
+        stream_unit<UNR, RAINW>(V, unit % SH.tiles_w, unit / SH.tiles_w, SH.strip_h, lane, s_sr[wid], s_sc[wid],
                              s_q0[wid], s_q1[wid], A);
     }
 

@@ -32,6 +32,7 @@ struct StreamView {
     int rows, cols, pitch, south_open;
     const float *Hin, *Uin, *Vin, *Zin, *Nin;  // Nin == nullptr: scalar Manning n
     const uint8_t *Min;
+    const float *Win;  // per-cell rain factors or nullptr (uniform rain)
     float *Hout, *Uout, *Vout;
     GridScalars<float> GS;
     Thr<float> T;
@@ -60,7 +61,9 @@ struct StreamAcc {
 
 // Advances column tile `ct`, row strip `rs` (strip height strip_h) of the
 // scenario in V.  s_sr/s_sc/s_q0/s_q1 are this warp's slots for local point
-// sources (kStreamMaxSrc each).  UNR is the unrolling of the row loop.
+// sources (kStreamMaxSrc each).  UNR is the unrolling of the row loop;
+// RAINW builds in the per-cell rain factors (V.Win), which the uniform-rain
+// build leaves out entirely (even unexecuted, that code slowed the loop).
 //
 // Domain edges need no tests of their own: the zero frame around every field
 // has mask 0, so the face tests on the two cells' masks already close the
@@ -71,7 +74,7 @@ struct StreamAcc {
 // face (cu:380-381), used by the open south edge.  Two rules of the
 // reference stay explicit: no cross advection u12 on column 0 (cu:178-180)
 // and no v11 on row 0 (cu:289-291).
-template <int UNR>
+template <int UNR, bool RAINW>
 __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, const int rs, const int strip_h,
                                             const int lane, int *s_sr, int *s_sc, float *s_q0, float *s_q1,
                                             StreamAcc &A) {
@@ -109,6 +112,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     const float *__restrict__ Zin = wuni(V.Zin);
     const float *__restrict__ Nin = wuni(V.Nin);
     const uint8_t *__restrict__ Min = wuni(V.Min);
+    const float *__restrict__ Win = wuni(V.Win);
     float *__restrict__ Hout = wuni(V.Hout);
     float *__restrict__ Uout = wuni(V.Uout);
     float *__restrict__ Vout = wuni(V.Vout);
@@ -264,7 +268,8 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
             const float pct = hi ? pct_hi : pct_lo;
             const float evapo = hi ? u_ev0 : 0.f;
             const float ql = nsrc ? source_at(r - 2, false) : 0.f;
-            const float rr = storm ? storm_rate(r - 2, on0, sx0, sy0) : u_rr0;
+            float rr = storm ? storm_rate(r - 2, on0, sx0, sy0) : u_rr0;
+            if (RAINW) rr = rr * Win[(r - 2) * pitch + gj];
             hs_2 = fmaxf(ho - dt2 * ((rum_1 - rum_2) * rdx + (rvnE_2 - rvn_2) * rdy - ql - rr * pct + evapo), 0.f);
         }
 
@@ -291,6 +296,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
             ev1 = hi ? u_ev1 : 0.f;
             ql1 = nsrc ? source_at(f, true) : 0.f;
             rr1 = storm ? storm_rate(f, on1, sx1, sy1) : u_rr1;
+            if (RAINW) rr1 = rr1 * Win[f * pitch + gj];
             hraw = ho - dt2 * ((us - un) * rdx + (ve - vw) * rdy - ql1 - rr1 * pct1 + ev1);
             hw_3 = fmaxf(hraw, 0.f);
         }

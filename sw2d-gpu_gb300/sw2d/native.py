@@ -83,6 +83,7 @@ _SIGS = {
     "sw2d_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "sw2d_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "sw2d_describe": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int32]),
+    "sw2d_set_rain_weights": (C.c_int, [C.c_void_p, C.c_void_p]),
     "sw2d_last_error": (C.c_char_p, [C.c_void_p]),
     "sw2d_status_string": (C.c_char_p, [C.c_int32]),
     "sw2d_volume_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_double,
@@ -217,6 +218,14 @@ class Solver:
 
     def set_storm(self, peak, x0, y0, vx, vy, sigma, t_stop=1e300):
         self._check(load().sw2d_set_storm(self._h, peak, x0, y0, vx, vy, sigma, t_stop), "sw2d_set_storm")
+
+    def set_rain_weights(self, w=None):
+        """Per-cell factors of the rain rate (rows x cols), or None for uniform rain."""
+        if w is None:
+            self._check(load().sw2d_set_rain_weights(self._h, None), "sw2d_set_rain_weights")
+            return
+        w = _f64(w, (self.rows, self.cols))
+        self._check(load().sw2d_set_rain_weights(self._h, _p(w)), "sw2d_set_rain_weights")
 
     def set_evaporation(self, series=None, dt_series=1.0):
         s = _f64(np.atleast_1d(series)) if series is not None else None
