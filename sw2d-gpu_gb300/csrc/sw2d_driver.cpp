@@ -23,6 +23,10 @@
 //   db/<case>/input/manning.txt         per-cell Manning n, ESRI ASCII of the
 //                                       DEM's shape (used when present; the
 //                                       reference has one scalar, cu:799)
+//   db/<case>/input/rain_weights.txt    spatial rain distribution: per-cell
+//                                       factors of rain.dat's rate, ESRI ASCII
+//                                       (used when present; the reference
+//                                       rains one value everywhere, cu:654)
 //   db/<case>/output/Outflow.txt        outflow hydrograph of the open south
 //                                       edge (--south-open): time, cumulative
 //                                       volume, mean rate since the last line
@@ -270,6 +274,12 @@ int run_case(const Opts &o, const std::string &name) {
         std::printf("unknown file - manning.txt\n");
         return 1;
     }
+    Esri rainw;
+    const bool has_w = file_exists(in + "rain_weights.txt");
+    if (has_w && (!read_esri(in + "rain_weights.txt", rainw) || rainw.rows != rows || rainw.cols != cols)) {
+        std::printf("unknown file - rain_weights.txt\n");
+        return 1;
+    }
     std::vector<double> ic = read_numbers(in + "initial_condition.txt");
     if (ic.size() < ncell) {
         std::printf("unknown file - initial_condition.txt\n");
@@ -318,6 +328,7 @@ int run_case(const Opts &o, const std::string &name) {
     sw2d_handle *h = nullptr;
     check(nullptr, sw2d_create(&cfg, &h), "sw2d_create");
     check(h, sw2d_set_static(h, dem.v.data(), has_n ? nman.v.data() : nullptr), "sw2d_set_static");
+    if (has_w) check(h, sw2d_set_rain_weights(h, rainw.v.data()), "sw2d_set_rain_weights");
     check(h, sw2d_set_state(h, ic.data(), nullptr, nullptr, time0), "sw2d_set_state");
     check(h, sw2d_set_rain(h, SW2D_RAIN_COMPAT, rain.data(), (int32_t)rain.size(), dtrain), "sw2d_set_rain");
     if (!evapo.empty())
