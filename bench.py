@@ -329,17 +329,22 @@ def depth_error(a, b, th=1.0e-4):
 
 def fp32_vs_fp64(sw2d, s, spun, dev, window=ACC_WINDOW_S):
     """FP32 and FP64 advanced from the same spun-up state to the same
-    simulated time (each with its own CFL steps); the depth error of FP32."""
+    simulated time (each with its own CFL steps); the depth error of FP32,
+    and beside it the FP64 run's own response to the rain rate raised by one
+    part in a million (the conditioning of the flow over the window)."""
     out = {}
-    for prec in (sw2d.PREC_F64, sw2d.PREC_F32):
+    for key, prec, scale in (("f64", sw2d.PREC_F64, 1.0), ("f32", sw2d.PREC_F32, 1.0),
+                             ("f64_rain_1e-6", sw2d.PREC_F64, 1.0 + 1e-6)):
         g = make_solver(sw2d, s, prec, dev)
+        g.set_rain(sw2d.RAIN_STEP, [RAIN_MM_H * scale], RAIN_HOURS * 3600.0)
         g.set_state(spun["h"], spun["um"], spun["vn"], t0=SPINUP_T)
         g.advance(10 ** 9, t_end=SPINUP_T + window)
-        out[prec] = (g.depth(), g.budget())
+        out[key] = (g.depth(), g.budget())
         g.close()
-    e = depth_error(out[sw2d.PREC_F64][0], out[sw2d.PREC_F32][0])
-    e.update({"window_s": window, "from_t_s": SPINUP_T, "steps_fp64": int(out[sw2d.PREC_F64][1]["steps"]),
-              "steps_fp32": int(out[sw2d.PREC_F32][1]["steps"])})
+    e = depth_error(out["f64"][0], out["f32"][0])
+    e.update({"window_s": window, "from_t_s": SPINUP_T, "steps_fp64": int(out["f64"][1]["steps"]),
+              "steps_fp32": int(out["f32"][1]["steps"]),
+              "fp64_vs_fp64_rain_1e-6": depth_error(out["f64"][0], out["f64_rain_1e-6"][0])})
     return e
 
 
