@@ -45,6 +45,7 @@ struct sw2d_handle {
     void *z = nullptr, *nman = nullptr;
     uint8_t *mask = nullptr;
     void *rainw = nullptr;  // spatial rain factors (allocated on first use)
+    void *dzx = nullptr, *dzy = nullptr;  // bed differences across faces (streaming kernel)
     bool use_rainw = false;
     double *stage = nullptr, *stage2 = nullptr;
     size_t stage_elems = 0;
@@ -126,6 +127,8 @@ StateBufs<Real> make_bufs(const sw2d_handle *h) {
     s.nman = h->has_nraster ? (const Real *)h->nman : nullptr;
     s.mask = h->mask;
     s.rainw = h->use_rainw ? (const Real *)h->rainw : nullptr;
+    s.dzx = (const Real *)h->dzx;
+    s.dzy = (const Real *)h->dzy;
     return s;
 }
 
@@ -291,7 +294,8 @@ int sw2d_device_bytes(const sw2d_config *c, int64_t *bytes) {
     size_t plane;
     grid_shape(c, &pitch, &plane, &th, &tw);
     const size_t rs = c->precision == SW2D_PREC_F64 ? 8 : 4;
-    size_t total = plane * rs * 8;  // 2x(h, um, vn) + z + n, frame included
+    const bool stream = c->precision == SW2D_PREC_F32 && c->kernel != SW2D_KERNEL_TILE;
+    size_t total = plane * rs * (stream ? 10 : 8);  // 2x(h, um, vn) + z + n (+ dzx, dzy), frame included
     total += plane;                 // mask
     total += 2 * (size_t)(c->rows + 1) * (c->cols + 1) * sizeof(double);  // staging
     total += kVolumeBlocks * sizeof(double) + 3 * sizeof(Clock) + sizeof(Control);
@@ -346,6 +350,8 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
     if (cudaMemset(h->d_clk, 0, 3 * sizeof(Clock)) != cudaSuccess) return bail(SW2D_ERR_CUDA);
     h->stream_kernel = cfg->precision == SW2D_PREC_F32 && cfg->kernel != SW2D_KERNEL_TILE;
     h->variant = cfg->variant;
+    if (h->stream_kernel && (!alloc_field(&h->dzx, h->real_size) || !alloc_field(&h->dzy, h->real_size)))
+        return bail(SW2D_ERR_OOM);
     if (h->stream_kernel) {
         e = prepare_stream_step(h->variant);
     } else {
@@ -413,6 +419,8 @@ int sw2d_destroy(sw2d_handle *h) {
     free_field(h->nman, h->real_size);
     free_field(h->mask, 1);
     free_field(h->rainw, h->real_size);
+    free_field(h->dzx, h->real_size);
+    free_field(h->dzy, h->real_size);
     cudaFree(h->stage);
     cudaFree(h->stage2);
     cudaFree(h->partial);
@@ -443,6 +451,8 @@ int sw2d_set_static(sw2d_handle *h, const double *z, const double *manning) {
     else
         CK(h, launch_pack_static(h->stage, dn, rows, cols, h->pitch, h->cfg.nodata, (float *)h->z,
                                  dn ? (float *)h->nman : nullptr, h->mask, h->stream));
+    if (h->stream_kernel)
+        CK(h, launch_pack_dz(h->stage, rows, cols, h->pitch, h->mask, (float *)h->dzx, (float *)h->dzy, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     h->has_nraster = manning != nullptr;
     h->have_static = true;

@@ -51,6 +51,28 @@ __global__ void pack_depth_kernel(const double *__restrict__ src, int rows, int 
     }
 }
 
+// Bed-elevation differences across the faces, for the FP32 streaming kernel:
+// dzx(i,j) = z(i,j) - z(i-1,j) on the x-face north of cell (i,j) and
+// dzy(i,j) = z(i,j) - z(i,j-1) on the y-face west of it, formed in FP64 from
+// the float64 DEM and rounded once; 0 on faces that are not between two active
+// cells.  The scheme uses the bed only through such differences (surface
+// slopes and the dry-bed rules), and a difference of a few centimetres taken
+// between two FP32 elevations near 100 m would carry their rounding (about
+// 4 um each) into every slope.
+template <class Real>
+__global__ void pack_dz_kernel(const double *__restrict__ z, int rows, int cols, int pitch,
+                               const uint8_t *__restrict__ mask, Real *__restrict__ dzx, Real *__restrict__ dzy) {
+    const long long total = (long long)rows * cols;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(k / cols), j = (int)(k - (k / cols) * cols);
+        const size_t gp = (size_t)i * pitch + j;
+        const bool m = mask[gp] != 0;
+        dzx[gp] = (i > 0 && m && mask[gp - pitch]) ? (Real)(z[k] - z[k - cols]) : Real(0);
+        dzy[gp] = (j > 0 && m && mask[gp - 1]) ? (Real)(z[k] - z[k - 1]) : Real(0);
+    }
+}
+
 // x-faces (rows+1) x cols.  A face is open only between two active cells or,
 // with an open south edge, below an active last-row cell; others are walls.
 template <class Real>

@@ -140,7 +140,7 @@ size_t scenario_bytes(const sw2d_config *c, int n_rain, bool raster) {
     const size_t plane = plane_for(c->rows, pitch);
     size_t s = 0;
     s += 6 * align256(plane * sizeof(float));                    // h, um, vn x 2
-    s += align256(plane * sizeof(float));                        // z
+    s += 3 * align256(plane * sizeof(float));                    // z, dzx, dzy
     if (raster) s += align256(plane * sizeof(float));            // n
     s += align256(plane);                                        // mask
     s += align256(3 * sizeof(Clock));                            // clock slots
@@ -277,6 +277,8 @@ int sw2d_batch_add(sw2d_batch *b, const sw2d_config *cfg, const double *z, const
     for (int k = 0; k < 2; k++) d.um[k] = carve<float>(base, off, plane) + org;
     for (int k = 0; k < 2; k++) d.vn[k] = carve<float>(base, off, plane) + org;
     float *z_dev = carve<float>(base, off, plane) + org;
+    float *dzx_dev = carve<float>(base, off, plane) + org;
+    float *dzy_dev = carve<float>(base, off, plane) + org;
     float *n_dev = raster ? carve<float>(base, off, plane) + org : nullptr;
     uint8_t *m_dev = carve<uint8_t>(base, off, plane) + org;
     Clock *clk = carve<Clock>(base, off, 3);
@@ -293,8 +295,9 @@ int sw2d_batch_add(sw2d_batch *b, const sw2d_config *cfg, const double *z, const
     double *st0 = b->d_stage, *st1 = b->d_stage + cells;
     BCK(b, cudaMemcpyAsync(st0, z, cells * sizeof(double), cudaMemcpyHostToDevice, b->stream));
     if (raster) BCK(b, cudaMemcpyAsync(st1, manning, cells * sizeof(double), cudaMemcpyHostToDevice, b->stream));
-    BCK(b, launch_pack_static(st0, raster ? st1 : nullptr, cfg->rows, cfg->cols, h.pitch, cfg->nodata, z_dev, n_dev,
-                              m_dev, b->stream));
+    BCK(b, launch_pack_static(st0, raster ? st1 : nullptr, cfg->rows, cfg->cols, h.pitch, cfg->nodata, z_dev,
+                              n_dev, m_dev, b->stream));
+    BCK(b, launch_pack_dz(st0, cfg->rows, cfg->cols, h.pitch, m_dev, dzx_dev, dzy_dev, b->stream));
     BCK(b, cudaMemcpyAsync(st0, depth, cells * sizeof(double), cudaMemcpyHostToDevice, b->stream));
     BCK(b, launch_pack_depth(st0, cfg->rows, cfg->cols, h.pitch, m_dev, d.h[0], b->stream));
     if (rain_kind != SW2D_RAIN_NONE)
@@ -357,6 +360,8 @@ int sw2d_batch_add(sw2d_batch *b, const sw2d_config *cfg, const double *z, const
     d.ctl.t_end = t_end;
     d.ctl.step_limit = 1ll << 62;
     d.z = z_dev;
+    d.dzx = dzx_dev;
+    d.dzy = dzy_dev;
     d.nman = n_dev;
     d.mask = m_dev;
     d.clk = clk;

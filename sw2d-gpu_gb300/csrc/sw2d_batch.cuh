@@ -37,7 +37,7 @@ struct ScenarioDev {
     Thr<float> T;
     Control ctl;
     float *h[2], *um[2], *vn[2];
-    const float *z, *nman;
+    const float *z, *dzx, *dzy, *nman;  // elevation, bed differences across faces, Manning n
     const uint8_t *mask;
     Clock *clk;                // three slots
     ScenarioStatus *status;    // this scenario's entry of the batch status array
@@ -93,7 +93,8 @@ __global__ void __launch_bounds__(NWARP * 32, MINB) batch_step_kernel(const Batc
             V.Hin = S.h[b];
             V.Uin = S.um[b];
             V.Vin = S.vn[b];
-            V.Zin = S.z;
+            V.DZX = S.dzx;
+            V.DZY = S.dzy;
             V.Nin = S.nman;
             V.Min = S.mask;
             V.Win = nullptr;  // batched scenarios rain uniformly

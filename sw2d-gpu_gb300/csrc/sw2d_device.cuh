@@ -145,6 +145,7 @@ struct StateBufs {
     const Real *nman;  // per-cell Manning n or nullptr
     const uint8_t *mask;
     const Real *rainw;  // per-cell factors of the rain rate, or nullptr (uniform rain)
+    const Real *dzx, *dzy;  // bed differences across x- / y-faces (streaming kernel only)
 };
 
 // wet/dry thresholds as `x >= c` constants (see file comment)

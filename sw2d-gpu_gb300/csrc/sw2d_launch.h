@@ -33,6 +33,8 @@ void default_tile(int precision, int *th, int *tw);
                             int slot, cudaStream_t st);                                                      \
     cudaError_t launch_pack_static(const double *z, const double *n, int rows, int cols, int pitch,         \
                                    double nodata, Real *zout, Real *nout, uint8_t *mask, cudaStream_t st);   \
+    cudaError_t launch_pack_dz(const double *z, int rows, int cols, int pitch, const uint8_t *mask, Real *dzx, \
+                               Real *dzy, cudaStream_t st);                                                  \
     cudaError_t launch_pack_depth(const double *src, int rows, int cols, int pitch, const uint8_t *mask,     \
                                   Real *dst, cudaStream_t st);                                               \
     cudaError_t launch_pack_um(const double *src, int rows, int cols, int pitch, int south_open,             \

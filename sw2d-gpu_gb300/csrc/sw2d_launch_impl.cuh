@@ -46,6 +46,13 @@ cudaError_t launch_pack_static(const double *z, const double *n, int rows, int c
     return cudaGetLastError();
 }
 
+cudaError_t launch_pack_dz(const double *z, int rows, int cols, int pitch, const uint8_t *mask, SW2D_REAL *dzx,
+                           SW2D_REAL *dzy, cudaStream_t st) {
+    pack_dz_kernel<SW2D_REAL><<<detail::grid_for((long long)rows * cols, 256), 256, 0, st>>>(z, rows, cols, pitch, mask,
+                                                                                           dzx, dzy);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_pack_depth(const double *src, int rows, int cols, int pitch, const uint8_t *mask,
                               SW2D_REAL *dst, cudaStream_t st) {
     pack_depth_kernel<SW2D_REAL><<<detail::grid_for((long long)rows * cols, 256), 256, 0, st>>>(

@@ -71,7 +71,8 @@ __global__ void __launch_bounds__(NWARP * 32, MINB)
         V.Hin = S.h[b];
         V.Uin = S.um[b];
         V.Vin = S.vn[b];
-        V.Zin = S.z;
+        V.DZX = S.dzx;
+        V.DZY = S.dzy;
         V.Nin = S.nman;
         V.Min = S.mask;
         V.Win = S.rainw;

@@ -27,10 +27,41 @@ __device__ __forceinline__ float shdn(float v) { return __shfl_down_sync(0xfffff
 __device__ __forceinline__ float upw(float vel2, float o, float s) { return vel2 * (vel2 >= 0.f ? s : o); }
 __device__ __forceinline__ float upw_r(float vel2, float o, float s) { return vel2 * (vel2 >= 0.f ? o : s); }
 
+// Dry-bed rules (cu:130-159 / cu:247-276) of a face between cells a (north /
+// west) and b, with the bed entering only as dz = z_b - z_a: the reference's
+// hb + zb < za is hb + dz < 0, ha + za < zb is ha < dz, and its
+// max(eta) - max(z) is max(hb + dz, ha) - max(dz, 0) (all shifted by z_a).
+// Returns true and sets q when a rule applies.
+__device__ __forceinline__ bool dry_bed_dz(const Thr<float> &T, float g, float ha, float hb, float dz, float &q) {
+    if (hb + dz < 0.f) {  // cu:130
+        q = (ha >= T.gt_th) ? 0.5440f * ha * sqrtf(g * ha) : 0.f;
+        return true;
+    }
+    if (ha < dz) {  // cu:138
+        q = (hb >= T.gt_th) ? -0.544f * hb * sqrtf(g * hb) : 0.f;
+        return true;
+    }
+    // cu:149: exactly one side strictly wet, with comparisons false for NaN
+    const bool b_wet = hb >= T.gt_th, a_wet = ha >= T.gt_th;
+    const bool b_dry = hb < T.ge_th, a_dry = ha < T.ge_th;
+    if ((b_wet && a_dry) || (b_dry && a_wet)) {
+        if ((hb > 0.f) || (ha > 0.f)) {
+            const float s = b_wet ? -0.350f : 0.350f;  // cu:151-154
+            const float hh3 = fmaxf(hb + dz, ha) - fmaxf(dz, 0.f);
+            q = s * hh3 * sqrtf(2.00f * g * hh3);
+        } else {
+            q = 0.f;
+        }
+        return true;
+    }
+    return false;
+}
+
 // Everything a warp reads to advance one strip of one scenario.
 struct StreamView {
     int rows, cols, pitch, south_open;
-    const float *Hin, *Uin, *Vin, *Zin, *Nin;  // Nin == nullptr: scalar Manning n
+    const float *Hin, *Uin, *Vin, *Nin;  // Nin == nullptr: scalar Manning n
+    const float *DZX, *DZY;              // bed differences across x- / y-faces (pack_dz_kernel)
     const uint8_t *Min;
     const float *Win;  // per-cell rain factors or nullptr (uniform rain)
     float *Hout, *Uout, *Vout;
@@ -109,7 +140,8 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     const float *__restrict__ Hin = wuni(V.Hin);
     const float *__restrict__ Uin = wuni(V.Uin);
     const float *__restrict__ Vin = wuni(V.Vin);
-    const float *__restrict__ Zin = wuni(V.Zin);
+    const float *__restrict__ DZX = wuni(V.DZX);
+    const float *__restrict__ DZY = wuni(V.DZY);
     const float *__restrict__ Nin = wuni(V.Nin);
     const uint8_t *__restrict__ Min = wuni(V.Min);
     const float *__restrict__ Win = wuni(V.Win);
@@ -172,12 +204,13 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     // row loads: rows R0-4 .. R1+2 and columns gj0 .. gj0+31 all lie inside
     // the zero frame around the domain, whose zeros are the inactive-cell and
     // wall values, so no load needs a bounds test
-    float p_h, p_z, p_n, p_um, p_vn;
+    float p_h, p_dzx, p_dzy, p_n, p_um, p_vn;
     unsigned p_m;
     int gp = (R0 - 4) * pitch + gj;  // element offset of the next row to read (fields fit 32-bit offsets)
     auto load_row = [&]() {
         p_h = Hin[gp];
-        p_z = Zin[gp];
+        p_dzx = DZX[gp];
+        p_dzy = DZY[gp];
         p_n = raster ? Nin[gp] : manning;
         p_m = (unsigned)Min[gp];
         p_um = Uin[gp];
@@ -187,7 +220,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
 
     // register rings: suffix = rows back from the row being read (r)
     float h1 = 0.f, h2 = 0.f, h3 = 0.f, hL1 = 0.f;
-    float z1 = 0.f, z2 = 0.f, zL1 = 0.f;
+    float dzx1 = 0.f, dzy1 = 0.f;  // bed differences of row r-1
     float n1 = manning, n2 = manning, nL1 = manning;
     float um1 = 0.f, um2 = 0.f, vn1 = 0.f, vn2 = 0.f;
     float uu_1 = 0.f, uu_2 = 0.f, uuL_1 = 0.f;
@@ -201,13 +234,13 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     load_row();
 #pragma unroll UNR
     for (int r = r_first; r < r_last; r++) {
-        const float h0 = p_h, z0 = p_z, n0 = p_n, um0 = p_um, vn0 = p_vn;
+        const float h0 = p_h, dzx0 = p_dzx, dzy0 = p_dzy, n0 = p_n, um0 = p_um, vn0 = p_vn;
         mb = (mb << 1) | p_m;
         const unsigned mL0 = __shfl_up_sync(0xffffffffu, p_m, 1);
         mLb = (mLb << 1) | mL0;
         if (r + 1 < r_last) load_row();  // prefetch the next row
 
-        const float hL0 = shup(h0), zL0 = shup(z0);
+        const float hL0 = shup(h0);
         const float nL0 = raster ? shup(n0) : manning;
         // ---- row r: face velocities (cu:363-453) ----
         const float hnf = 0.50f * (h0 + hL0);
@@ -224,11 +257,11 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         const float vvW = shup(vv_1);
         float rum_1 = 0.f;
         {
-            const float ha = h2, hb = h1, za = z2, zb = z1;
+            const float ha = h2, hb = h1, dz = dzx1;
             if (((mb >> 2) & (mb >> 1) & 1u) && ((ha >= gt_th) || (hb >= gt_th))) {
-                if (!dry_bed<float>(T, g, ha, za, hb, zb, rum_1)) {
+                if (!dry_bed_dz(T, g, ha, hb, dz, rum_1)) {
                     const float hm = 0.50f * (hb + ha);
-                    const float u13 = g * hm * dt2dx * (hb + zb - ha - za);  // cu:166
+                    const float u13 = g * hm * dt2dx * ((hb - ha) + dz);  // cu:166, hb + zb - ha - za
                     const float u11 = hdx * (upw(uu_0 + uu_1, um0, um1) - upw_r(uu_1 + uu_2, um2, um1));
                     const float u12c = hdy * (upw(vvR_1 + vvR_2, umE, um1) - upw_r(vv_1 + vv_2, umW, um1));
                     const float u12 = not_col0 ? u12c : 0.f;  // zero on column 0 (cu:178-180)
@@ -243,11 +276,11 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         }
         float rvn_1 = 0.f;
         {
-            const float ha = hL1, hb = h1, za = zL1, zb = z1;
+            const float ha = hL1, hb = h1, dz = dzy1;
             if (((mLb >> 1) & (mb >> 1) & 1u) && ((ha >= gt_th) || (hb >= gt_th))) {
-                if (!dry_bed<float>(T, g, ha, za, hb, zb, rvn_1)) {
+                if (!dry_bed_dz(T, g, ha, hb, dz, rvn_1)) {
                     const float hn = 0.50f * (hb + ha);
-                    const float v13 = g * hn * dt2dy * (hb + zb - ha - za);  // cu:283
+                    const float v13 = g * hn * dt2dy * ((hb - ha) + dz);  // cu:283, hb + zb - ha - za
                     const float v11c = hdx * (upw(uu_0 + uuL_0, vn0, vn1) - upw_r(uu_1 + uuL_1, vn2, vn1));
                     const float v11 = (i != 0) ? v11c : 0.f;  // zero on row 0 (cu:289-291)
                     const float v12 = hdy * (upw(vvR_1 + vv_1, vnE, vn1) - upw_r(vv_1 + vvW, vnW, vn1));
@@ -333,7 +366,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
 
         // ---- advance the rings ----
         h3 = h2; h2 = h1; h1 = h0; hL1 = hL0;
-        z2 = z1; z1 = z0; zL1 = zL0;
+        dzx1 = dzx0; dzy1 = dzy0;
         n2 = n1; n1 = n0; nL1 = nL0;
         um2 = um1; um1 = um0; vn2 = vn1; vn1 = vn0;
         uu_2 = uu_1; uu_1 = uu_0; uuL_1 = uuL_0;

@@ -61,7 +61,10 @@ def test_f32_catchment_rain_vs_oracle(oracle_mod, sw2d_mod, kernel):
 
 
 def test_stream_matches_tile_kernel(sw2d_mod):
-    """Same scheme, same precision, two kernel organisations."""
+    """Same scheme, same precision, two kernel organisations.  The streaming
+    kernel forms the bed slopes from face differences taken in FP64, the tile
+    kernel from FP32 elevations, so they agree to the FP32 bound, not to the
+    last bit."""
     s, z = _catchment(seed=4, rows=70, cols=130)
     g1 = _f32(sw2d_mod, 70, 130, 5.0, z, s["h0"], n=s["n"], kernel=1, south_open=1, dt_mode=1, dt=2.0)
     g2 = _f32(sw2d_mod, 70, 130, 5.0, z, s["h0"], n=s["n"], kernel=2, south_open=1, dt_mode=1, dt=2.0, strip_h=16)
@@ -70,7 +73,7 @@ def test_stream_matches_tile_kernel(sw2d_mod):
         assert g.advance(300) == 300
     b1, b2 = g1.budget(), g2.budget()
     assert abs(b1["t"] - b2["t"]) <= 1e-6 * b1["t"]
-    assert max_abs(g1.depth(), g2.depth()) <= 1e-4
+    assert max_abs(g1.depth(), g2.depth()) <= TOL_MM
 
 
 @pytest.mark.parametrize("strip_h", [1, 7, 16, 64, 128])
