@@ -46,6 +46,7 @@ struct sw2d_handle {
     uint8_t *mask = nullptr;
     void *rainw = nullptr;  // spatial rain factors (allocated on first use)
     void *dzx = nullptr, *dzy = nullptr;  // bed differences across faces (streaming kernel)
+    void *hr[2] = {nullptr, nullptr};      // depth remainders of the compensated FP32 state (streaming kernel)
     bool use_rainw = false;
     double *stage = nullptr, *stage2 = nullptr;
     size_t stage_elems = 0;
@@ -127,6 +128,8 @@ StateBufs<Real> make_bufs(const sw2d_handle *h) {
     s.nman = h->has_nraster ? (const Real *)h->nman : nullptr;
     s.mask = h->mask;
     s.rainw = h->use_rainw ? (const Real *)h->rainw : nullptr;
+    s.hr[0] = (Real *)h->hr[0];
+    s.hr[1] = (Real *)h->hr[1];
     s.dzx = (const Real *)h->dzx;
     s.dzy = (const Real *)h->dzy;
     return s;
@@ -295,7 +298,7 @@ int sw2d_device_bytes(const sw2d_config *c, int64_t *bytes) {
     grid_shape(c, &pitch, &plane, &th, &tw);
     const size_t rs = c->precision == SW2D_PREC_F64 ? 8 : 4;
     const bool stream = c->precision == SW2D_PREC_F32 && c->kernel != SW2D_KERNEL_TILE;
-    size_t total = plane * rs * (stream ? 10 : 8);  // 2x(h, um, vn) + z + n (+ dzx, dzy), frame included
+    size_t total = plane * rs * (stream ? 12 : 8);  // 2x(h, um, vn) + z + n (+ dzx, dzy, 2x remainder), frame included
     total += plane;                 // mask
     total += 2 * (size_t)(c->rows + 1) * (c->cols + 1) * sizeof(double);  // staging
     total += kVolumeBlocks * sizeof(double) + 3 * sizeof(Clock) + sizeof(Control);
@@ -350,7 +353,8 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
     if (cudaMemset(h->d_clk, 0, 3 * sizeof(Clock)) != cudaSuccess) return bail(SW2D_ERR_CUDA);
     h->stream_kernel = cfg->precision == SW2D_PREC_F32 && cfg->kernel != SW2D_KERNEL_TILE;
     h->variant = cfg->variant;
-    if (h->stream_kernel && (!alloc_field(&h->dzx, h->real_size) || !alloc_field(&h->dzy, h->real_size)))
+    if (h->stream_kernel && (!alloc_field(&h->dzx, h->real_size) || !alloc_field(&h->dzy, h->real_size) ||
+                             !alloc_field(&h->hr[0], h->real_size) || !alloc_field(&h->hr[1], h->real_size)))
         return bail(SW2D_ERR_OOM);
     if (h->stream_kernel) {
         e = prepare_stream_step(h->variant);
@@ -420,6 +424,8 @@ int sw2d_destroy(sw2d_handle *h) {
     free_field(h->mask, 1);
     free_field(h->rainw, h->real_size);
     free_field(h->dzx, h->real_size);
+    free_field(h->hr[0], h->real_size);
+    free_field(h->hr[1], h->real_size);
     free_field(h->dzy, h->real_size);
     cudaFree(h->stage);
     cudaFree(h->stage2);
@@ -501,6 +507,7 @@ int sw2d_set_state(sw2d_handle *h, const double *depth, const double *um, const 
         CK(h, cudaMemsetAsync(raw_field(h, h->h[b]), 0, fb, h->stream));
         CK(h, cudaMemsetAsync(raw_field(h, h->um[b]), 0, fb, h->stream));
         CK(h, cudaMemsetAsync(raw_field(h, h->vn[b]), 0, fb, h->stream));
+        if (h->hr[b]) CK(h, cudaMemsetAsync(raw_field(h, h->hr[b]), 0, fb, h->stream));
     }
     CK(h, cudaMemcpyAsync(h->stage, depth, (size_t)rows * cols * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     if (is_f64(h)) CK(h, launch_pack_depth(h->stage, rows, cols, pitch, h->mask, (double *)h->h[0], h->stream));
@@ -682,9 +689,9 @@ int sw2d_get_field(sw2d_handle *h, int32_t field, double *out) {
     const int b = h->clock.buf;
     const bool f64 = is_f64(h);
     int nr = rows, nc = cols;
-    const void *src = nullptr;
+    const void *src = nullptr, *add = nullptr;
     switch (field) {
-    case SW2D_FIELD_DEPTH: src = h->h[b]; break;
+    case SW2D_FIELD_DEPTH: src = h->h[b]; add = h->hr[b]; break;
     case SW2D_FIELD_UM: src = h->um[b]; nr = rows + 1; break;
     case SW2D_FIELD_VN: src = h->vn[b]; nc = cols + 1; break;
     case SW2D_FIELD_ELEVATION: src = h->z; break;
@@ -704,8 +711,8 @@ int sw2d_get_field(sw2d_handle *h, int32_t field, double *out) {
     default:
         return fail(h, SW2D_ERR_INVALID_ARG, "unknown field");
     }
-    if (f64) CK(h, launch_unpack((const double *)src, nr, nc, pitch, h->stage, h->stream));
-    else CK(h, launch_unpack((const float *)src, nr, nc, pitch, h->stage, h->stream));
+    if (f64) CK(h, launch_unpack((const double *)src, (const double *)add, nr, nc, pitch, h->stage, h->stream));
+    else CK(h, launch_unpack((const float *)src, (const float *)add, nr, nc, pitch, h->stage, h->stream));
     CK(h, cudaMemcpyAsync(out, h->stage, (size_t)nr * nc * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     return SW2D_OK;
@@ -716,11 +723,11 @@ int sw2d_get_budget(sw2d_handle *h, sw2d_budget *out) {
     if (!h->have_state) return fail(h, SW2D_ERR_STATE, "no state");
     const int b = h->clock.buf;
     if (is_f64(h))
-        CK(h, launch_volume((const double *)h->h[b], h->mask, h->cfg.rows, h->cfg.cols, h->pitch, h->partial,
-                            kVolumeBlocks, h->stream));
+        CK(h, launch_volume((const double *)h->h[b], nullptr, h->mask, h->cfg.rows, h->cfg.cols, h->pitch,
+                            h->partial, kVolumeBlocks, h->stream));
     else
-        CK(h, launch_volume((const float *)h->h[b], h->mask, h->cfg.rows, h->cfg.cols, h->pitch, h->partial,
-                            kVolumeBlocks, h->stream));
+        CK(h, launch_volume((const float *)h->h[b], (const float *)h->hr[b], h->mask, h->cfg.rows, h->cfg.cols,
+                            h->pitch, h->partial, kVolumeBlocks, h->stream));
     CK(h, cudaMemcpyAsync(h->h_partial, h->partial, kVolumeBlocks * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     double s = 0.0, c = 0.0;
@@ -767,11 +774,11 @@ int sw2d_probe(sw2d_handle *h, const int32_t *cells, int32_t n, double *out) {
     }
     const int b = h->clock.buf;
     if (is_f64(h))
-        CK(h, launch_probe((const double *)h->h[b], h->cfg.rows, h->cfg.cols, h->pitch, (const int *)h->probe_cells.p, n,
-                           (double *)h->probe_out.p, h->stream));
+        CK(h, launch_probe((const double *)h->h[b], nullptr, h->cfg.rows, h->cfg.cols, h->pitch,
+                           (const int *)h->probe_cells.p, n, (double *)h->probe_out.p, h->stream));
     else
-        CK(h, launch_probe((const float *)h->h[b], h->cfg.rows, h->cfg.cols, h->pitch, (const int *)h->probe_cells.p, n,
-                           (double *)h->probe_out.p, h->stream));
+        CK(h, launch_probe((const float *)h->h[b], (const float *)h->hr[b], h->cfg.rows, h->cfg.cols, h->pitch,
+                           (const int *)h->probe_cells.p, n, (double *)h->probe_out.p, h->stream));
     CK(h, cudaMemcpyAsync(out, h->probe_out.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     return SW2D_OK;
@@ -781,15 +788,17 @@ namespace {
 struct CheckpointHeader {
     char magic[8];  // "SW2DCKP1"
     int32_t rows, cols, pitch, precision;
+    int32_t nplanes, pad;  // h, um, vn (+ the depth remainder of the compensated FP32 state)
     int64_t plane_bytes;
     double volume0;
     Clock clock;
 };
+int checkpoint_planes(const sw2d_handle *h) { return h->hr[0] ? 4 : 3; }
 }  // namespace
 
 int sw2d_checkpoint_bytes(sw2d_handle *h, int64_t *bytes) {
     if (!h || !bytes) return SW2D_ERR_INVALID_ARG;
-    *bytes = (int64_t)(sizeof(CheckpointHeader) + 3 * h->plane * h->real_size);
+    *bytes = (int64_t)(sizeof(CheckpointHeader) + checkpoint_planes(h) * h->plane * h->real_size);
     return SW2D_OK;
 }
 
@@ -809,14 +818,16 @@ int sw2d_checkpoint_save(sw2d_handle *h, void *buf, int64_t bytes) {
     hd.pitch = h->pitch;
     hd.precision = h->cfg.precision;
     hd.plane_bytes = (int64_t)(h->plane * h->real_size);
+    hd.nplanes = checkpoint_planes(h);
     hd.volume0 = h->volume0;
     hd.clock = h->clock;
     char *p = static_cast<char *>(buf);
     std::memcpy(p, &hd, sizeof(hd));
     p += sizeof(hd);
     const int b = h->clock.buf;
-    void *src[3] = {raw_field(h, h->h[b]), raw_field(h, h->um[b]), raw_field(h, h->vn[b])};
-    for (int k = 0; k < 3; k++) {
+    void *src[4] = {raw_field(h, h->h[b]), raw_field(h, h->um[b]), raw_field(h, h->vn[b]),
+                    h->hr[b] ? raw_field(h, h->hr[b]) : nullptr};
+    for (int k = 0; k < hd.nplanes; k++) {
         CK(h, cudaMemcpyAsync(p, src[k], (size_t)hd.plane_bytes, cudaMemcpyDeviceToHost, h->stream));
         p += hd.plane_bytes;
     }
@@ -833,11 +844,13 @@ int sw2d_checkpoint_load(sw2d_handle *h, const void *buf, int64_t bytes) {
     int64_t need = 0;
     sw2d_checkpoint_bytes(h, &need);
     if (std::memcmp(hd.magic, "SW2DCKP1", 8) != 0 || hd.rows != h->cfg.rows || hd.cols != h->cfg.cols ||
-        hd.pitch != h->pitch || hd.precision != h->cfg.precision || bytes < need)
+        hd.pitch != h->pitch || hd.precision != h->cfg.precision || hd.nplanes != checkpoint_planes(h) ||
+        bytes < need)
         return fail(h, SW2D_ERR_INVALID_ARG, "checkpoint does not match this handle's config");
     const char *p = static_cast<const char *>(buf) + sizeof(hd);
-    void *dst[3] = {raw_field(h, h->h[0]), raw_field(h, h->um[0]), raw_field(h, h->vn[0])};
-    for (int k = 0; k < 3; k++) {
+    void *dst[4] = {raw_field(h, h->h[0]), raw_field(h, h->um[0]), raw_field(h, h->vn[0]),
+                    h->hr[0] ? raw_field(h, h->hr[0]) : nullptr};
+    for (int k = 0; k < hd.nplanes; k++) {
         CK(h, cudaMemcpyAsync(dst[k], p, (size_t)hd.plane_bytes, cudaMemcpyHostToDevice, h->stream));
         p += hd.plane_bytes;
     }
@@ -845,6 +858,7 @@ int sw2d_checkpoint_load(sw2d_handle *h, const void *buf, int64_t bytes) {
     CK(h, cudaMemsetAsync(raw_field(h, h->h[1]), 0, fb, h->stream));
     CK(h, cudaMemsetAsync(raw_field(h, h->um[1]), 0, fb, h->stream));
     CK(h, cudaMemsetAsync(raw_field(h, h->vn[1]), 0, fb, h->stream));
+    if (h->hr[1]) CK(h, cudaMemsetAsync(raw_field(h, h->hr[1]), 0, fb, h->stream));
     // the saved clock becomes slot 0 of a fresh launch sequence
     Clock c = hd.clock;
     c.buf = 0;

@@ -107,12 +107,14 @@ __global__ void pack_vn_kernel(const double *__restrict__ src, int rows, int col
 
 // nr x nc window of a pitched array -> compact float64
 template <class Real>
-__global__ void unpack_kernel(const Real *__restrict__ src, int nr, int nc, int pitch, double *__restrict__ dst) {
+__global__ void unpack_kernel(const Real *__restrict__ src, const Real *__restrict__ add, int nr, int nc, int pitch,
+                              double *__restrict__ dst) {
     const long long total = (long long)nr * nc;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
          k += (long long)gridDim.x * blockDim.x) {
         const int i = (int)(k / nc), j = (int)(k - (k / nc) * nc);
-        dst[k] = (double)src[(size_t)i * pitch + j];
+        const size_t gp = (size_t)i * pitch + j;
+        dst[k] = (double)src[gp] + (add ? (double)add[gp] : 0.0);  // add: the depth's remainder plane
     }
 }
 
@@ -165,7 +167,8 @@ __global__ void velocity_kernel(const Real *__restrict__ h, const Real *__restri
 // fixed per-thread order, so the result is deterministic; the host adds the
 // partials with Kahan summation.
 template <class Real, int NT>
-__global__ void __launch_bounds__(NT) volume_kernel(const Real *__restrict__ h, const uint8_t *__restrict__ mask,
+__global__ void __launch_bounds__(NT) volume_kernel(const Real *__restrict__ h, const Real *__restrict__ hr,
+                                                    const uint8_t *__restrict__ mask,
                                                     int rows, int cols, int pitch, double *__restrict__ partial) {
     __shared__ double s[NT / 32];
     const long long total = (long long)rows * cols;
@@ -174,7 +177,7 @@ __global__ void __launch_bounds__(NT) volume_kernel(const Real *__restrict__ h, 
         const int i = (int)(k / cols), j = (int)(k - (k / cols) * cols);
         const size_t gp = (size_t)i * pitch + j;
         if (mask[gp]) {
-            const double y = (double)h[gp] - comp;
+            const double y = ((double)h[gp] + (hr ? (double)hr[gp] : 0.0)) - comp;
             const double t = acc + y;
             comp = (t - acc) - y;
             acc = t;
@@ -222,8 +225,8 @@ __global__ void cmax_kernel(const Real *__restrict__ h, const Real *__restrict__
 }
 
 template <class Real>
-__global__ void probe_kernel(const Real *__restrict__ h, int rows, int cols, int pitch, const int *__restrict__ cells,
-                             int n, double *__restrict__ out) {
+__global__ void probe_kernel(const Real *__restrict__ h, const Real *__restrict__ hr, int rows, int cols, int pitch,
+                             const int *__restrict__ cells, int n, double *__restrict__ out) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int c = cells[k];
@@ -232,7 +235,8 @@ __global__ void probe_kernel(const Real *__restrict__ h, int rows, int cols, int
         return;
     }
     const int i = c / cols, j = c - (c / cols) * cols;
-    out[k] = (double)h[(size_t)i * pitch + j];
+    const size_t gp = (size_t)i * pitch + j;
+    out[k] = (double)h[gp] + (hr ? (double)hr[gp] : 0.0);
 }
 
 }  // namespace sw2d

@@ -139,7 +139,7 @@ size_t scenario_bytes(const sw2d_config *c, int n_rain, bool raster) {
     const int pitch = pitch_for(c->cols);
     const size_t plane = plane_for(c->rows, pitch);
     size_t s = 0;
-    s += 6 * align256(plane * sizeof(float));                    // h, um, vn x 2
+    s += 8 * align256(plane * sizeof(float));                    // h, um, vn, depth remainder x 2
     s += 3 * align256(plane * sizeof(float));                    // z, dzx, dzy
     if (raster) s += align256(plane * sizeof(float));            // n
     s += align256(plane);                                        // mask
@@ -276,6 +276,7 @@ int sw2d_batch_add(sw2d_batch *b, const sw2d_config *cfg, const double *z, const
     for (int k = 0; k < 2; k++) d.h[k] = carve<float>(base, off, plane) + org;
     for (int k = 0; k < 2; k++) d.um[k] = carve<float>(base, off, plane) + org;
     for (int k = 0; k < 2; k++) d.vn[k] = carve<float>(base, off, plane) + org;
+    for (int k = 0; k < 2; k++) d.hr[k] = carve<float>(base, off, plane) + org;
     float *z_dev = carve<float>(base, off, plane) + org;
     float *dzx_dev = carve<float>(base, off, plane) + org;
     float *dzy_dev = carve<float>(base, off, plane) + org;
@@ -464,16 +465,16 @@ int sw2d_batch_get_field(sw2d_batch *b, int32_t id, int32_t field, double *out) 
     const int buf = b->h_clk->buf;
     const int rows = h.cfg.rows, cols = h.cfg.cols;
     int nr = rows, nc = cols;
-    const float *src = nullptr;
+    const float *src = nullptr, *add = nullptr;
     switch (field) {
-    case SW2D_FIELD_DEPTH: src = h.dev.h[buf]; break;
+    case SW2D_FIELD_DEPTH: src = h.dev.h[buf]; add = h.dev.hr[buf]; break;
     case SW2D_FIELD_UM: src = h.dev.um[buf]; nr = rows + 1; break;
     case SW2D_FIELD_VN: src = h.dev.vn[buf]; nc = cols + 1; break;
     case SW2D_FIELD_ELEVATION: src = h.dev.z; break;
     default: return bfail(b, SW2D_ERR_INVALID_ARG, "field not available for batched scenarios");
     }
     if (b->stage_elems < (size_t)nr * nc) return bfail(b, SW2D_ERR_STATE, "staging buffer too small");
-    BCK(b, launch_unpack(src, nr, nc, h.pitch, b->d_stage, b->stream));
+    BCK(b, launch_unpack(src, add, nr, nc, h.pitch, b->d_stage, b->stream));
     BCK(b, cudaMemcpyAsync(out, b->d_stage, (size_t)nr * nc * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
     BCK(b, cudaStreamSynchronize(b->stream));
     return SW2D_OK;
@@ -486,7 +487,7 @@ int sw2d_batch_get_budget(sw2d_batch *b, int32_t id, sw2d_budget *out) {
     int rc = read_current_clock(b, h);
     if (rc) return rc;
     const Clock k = *b->h_clk;
-    BCK(b, launch_volume(h.dev.h[k.buf], h.dev.mask, h.cfg.rows, h.cfg.cols, h.pitch, b->d_partial, kVolumeBlocks,
+    BCK(b, launch_volume(h.dev.h[k.buf], h.dev.hr[k.buf], h.dev.mask, h.cfg.rows, h.cfg.cols, h.pitch, b->d_partial, kVolumeBlocks,
                          b->stream));
     BCK(b, cudaMemcpyAsync(b->h_partial, b->d_partial, kVolumeBlocks * sizeof(double), cudaMemcpyDeviceToHost,
                            b->stream));

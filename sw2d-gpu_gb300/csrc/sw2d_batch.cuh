@@ -36,7 +36,7 @@ struct ScenarioDev {
     ForcingDesc F;
     Thr<float> T;
     Control ctl;
-    float *h[2], *um[2], *vn[2];
+    float *h[2], *um[2], *vn[2], *hr[2];  // hr: depth remainders (compensated depth)
     const float *z, *dzx, *dzy, *nman;  // elevation, bed differences across faces, Manning n
     const uint8_t *mask;
     Clock *clk;                // three slots
@@ -95,6 +95,8 @@ __global__ void __launch_bounds__(NWARP * 32, MINB) batch_step_kernel(const Batc
             V.Vin = S.vn[b];
             V.DZX = S.dzx;
             V.DZY = S.dzy;
+            V.Rin = S.hr[b];
+            V.Rout = S.hr[1 - b];
             V.Nin = S.nman;
             V.Min = S.mask;
             V.Win = nullptr;  // batched scenarios rain uniformly

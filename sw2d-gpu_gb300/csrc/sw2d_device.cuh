@@ -146,6 +146,7 @@ struct StateBufs {
     const uint8_t *mask;
     const Real *rainw;  // per-cell factors of the rain rate, or nullptr (uniform rain)
     const Real *dzx, *dzy;  // bed differences across x- / y-faces (streaming kernel only)
+    Real *hr[2];            // depth remainders of the compensated FP32 state (streaming kernel only)
 };
 
 // wet/dry thresholds as `x >= c` constants (see file comment)

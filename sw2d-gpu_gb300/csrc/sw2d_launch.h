@@ -41,15 +41,16 @@ void default_tile(int precision, int *th, int *tw);
                                const uint8_t *mask, Real *dst, cudaStream_t st);                             \
     cudaError_t launch_pack_vn(const double *src, int rows, int cols, int pitch, const uint8_t *mask,        \
                                Real *dst, cudaStream_t st);                                                  \
-    cudaError_t launch_unpack(const Real *src, int nr, int nc, int pitch, double *dst, cudaStream_t st);     \
+    cudaError_t launch_unpack(const Real *src, const Real *add, int nr, int nc, int pitch, double *dst,    \
+                              cudaStream_t st);                                                          \
     cudaError_t launch_velocity(const Real *h, const Real *um, const Real *vn, int rows, int cols, int pitch, \
                                 Real ge_th, double *uu, double *vv, cudaStream_t st);                        \
-    cudaError_t launch_volume(const Real *h, const uint8_t *mask, int rows, int cols, int pitch,             \
+    cudaError_t launch_volume(const Real *h, const Real *hr, const uint8_t *mask, int rows, int cols, int pitch, \
                               double *partial, int nblocks, cudaStream_t st);                                \
     cudaError_t launch_cmax(const Real *h, const Real *um, const Real *vn, const uint8_t *mask, int rows,    \
                             int cols, int pitch, int south_open, Real ge_th, double g,                       \
                             unsigned long long *out, cudaStream_t st);                                       \
-    cudaError_t launch_probe(const Real *h, int rows, int cols, int pitch, const int *cells, int n,          \
+    cudaError_t launch_probe(const Real *h, const Real *hr, int rows, int cols, int pitch, const int *cells, int n, \
                              double *out, cudaStream_t st);
 
 SW2D_DECLARE_LAUNCHERS(double)

@@ -74,8 +74,9 @@ cudaError_t launch_pack_vn(const double *src, int rows, int cols, int pitch, con
     return cudaGetLastError();
 }
 
-cudaError_t launch_unpack(const SW2D_REAL *src, int nr, int nc, int pitch, double *dst, cudaStream_t st) {
-    unpack_kernel<SW2D_REAL><<<detail::grid_for((long long)nr * nc, 256), 256, 0, st>>>(src, nr, nc, pitch, dst);
+cudaError_t launch_unpack(const SW2D_REAL *src, const SW2D_REAL *add, int nr, int nc, int pitch, double *dst,
+                          cudaStream_t st) {
+    unpack_kernel<SW2D_REAL><<<detail::grid_for((long long)nr * nc, 256), 256, 0, st>>>(src, add, nr, nc, pitch, dst);
     return cudaGetLastError();
 }
 
@@ -86,9 +87,9 @@ cudaError_t launch_velocity(const SW2D_REAL *h, const SW2D_REAL *um, const SW2D_
     return cudaGetLastError();
 }
 
-cudaError_t launch_volume(const SW2D_REAL *h, const uint8_t *mask, int rows, int cols, int pitch,
+cudaError_t launch_volume(const SW2D_REAL *h, const SW2D_REAL *hr, const uint8_t *mask, int rows, int cols, int pitch,
                           double *partial, int nblocks, cudaStream_t st) {
-    volume_kernel<SW2D_REAL, kVolumeThreads><<<nblocks, kVolumeThreads, 0, st>>>(h, mask, rows, cols, pitch,
+    volume_kernel<SW2D_REAL, kVolumeThreads><<<nblocks, kVolumeThreads, 0, st>>>(h, hr, mask, rows, cols, pitch,
                                                                                   partial);
     return cudaGetLastError();
 }
@@ -101,10 +102,10 @@ cudaError_t launch_cmax(const SW2D_REAL *h, const SW2D_REAL *um, const SW2D_REAL
     return cudaGetLastError();
 }
 
-cudaError_t launch_probe(const SW2D_REAL *h, int rows, int cols, int pitch, const int *cells, int n,
-                         double *out, cudaStream_t st) {
+cudaError_t launch_probe(const SW2D_REAL *h, const SW2D_REAL *hr, int rows, int cols, int pitch, const int *cells,
+                         int n, double *out, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    probe_kernel<SW2D_REAL><<<(n + 255) / 256, 256, 0, st>>>(h, rows, cols, pitch, cells, n, out);
+    probe_kernel<SW2D_REAL><<<(n + 255) / 256, 256, 0, st>>>(h, hr, rows, cols, pitch, cells, n, out);
     return cudaGetLastError();
 }
 

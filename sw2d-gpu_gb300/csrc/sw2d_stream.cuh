@@ -73,6 +73,8 @@ __global__ void __launch_bounds__(NWARP * 32, MINB)
         V.Vin = S.vn[b];
         V.DZX = S.dzx;
         V.DZY = S.dzy;
+        V.Rin = S.hr[b];
+        V.Rout = S.hr[1 - b];
         V.Nin = S.nman;
         V.Min = S.mask;
         V.Win = S.rainw;

@@ -27,6 +27,13 @@ __device__ __forceinline__ float shdn(float v) { return __shfl_down_sync(0xfffff
 __device__ __forceinline__ float upw(float vel2, float o, float s) { return vel2 * (vel2 >= 0.f ? s : o); }
 __device__ __forceinline__ float upw_r(float vel2, float o, float s) { return vel2 * (vel2 >= 0.f ? o : s); }
 
+// s + e = a + b exactly when |a| >= |b| or a == 0 (Dekker's fast two-sum,
+// written without contraction or reassociation).
+__device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
 // Dry-bed rules (cu:130-159 / cu:247-276) of a face between cells a (north /
 // west) and b, with the bed entering only as dz = z_b - z_a: the reference's
 // hb + zb < za is hb + dz < 0, ha + za < zb is ha < dz, and its
@@ -62,6 +69,8 @@ struct StreamView {
     int rows, cols, pitch, south_open;
     const float *Hin, *Uin, *Vin, *Nin;  // Nin == nullptr: scalar Manning n
     const float *DZX, *DZY;              // bed differences across x- / y-faces (pack_dz_kernel)
+    const float *Rin;                    // depth remainders of the state read (compensated depth)
+    float *Rout;                         // and of the state written
     const uint8_t *Min;
     const float *Win;  // per-cell rain factors or nullptr (uniform rain)
     float *Hout, *Uout, *Vout;
@@ -142,6 +151,8 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     const float *__restrict__ Vin = wuni(V.Vin);
     const float *__restrict__ DZX = wuni(V.DZX);
     const float *__restrict__ DZY = wuni(V.DZY);
+    const float *__restrict__ Rin = wuni(V.Rin);
+    float *__restrict__ Rout = wuni(V.Rout);
     const float *__restrict__ Nin = wuni(V.Nin);
     const uint8_t *__restrict__ Min = wuni(V.Min);
     const float *__restrict__ Win = wuni(V.Win);
@@ -204,11 +215,14 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     // row loads: rows R0-4 .. R1+2 and columns gj0 .. gj0+31 all lie inside
     // the zero frame around the domain, whose zeros are the inactive-cell and
     // wall values, so no load needs a bounds test
-    float p_h, p_dzx, p_dzy, p_n, p_um, p_vn;
+    float p_h, p_dzx, p_dzy, p_n, p_um, p_vn, p_res;
     unsigned p_m;
     int gp = (R0 - 4) * pitch + gj;  // element offset of the next row to read (fields fit 32-bit offsets)
+    int lrow = R0 - 4;  // row of the next load
     auto load_row = [&]() {
         p_h = Hin[gp];
+        p_res = lrow >= 3 ? Rin[gp - 3 * pitch] : 0.f;  // remainder of row lrow-3, used with this row
+        lrow++;
         p_dzx = DZX[gp];
         p_dzy = DZY[gp];
         p_n = raster ? Nin[gp] : manning;
@@ -235,6 +249,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
 #pragma unroll UNR
     for (int r = r_first; r < r_last; r++) {
         const float h0 = p_h, dzx0 = p_dzx, dzy0 = p_dzy, n0 = p_n, um0 = p_um, vn0 = p_vn;
+        const float res3 = p_res;  // depth remainder of row r-3
         mb = (mb << 1) | p_m;
         const unsigned mL0 = __shfl_up_sync(0xffffffffu, p_m, 1);
         mLb = (mLb << 1) | mL0;
@@ -321,7 +336,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         if ((vw > 0.f && dW3) || (vw < 0.f && d3)) vw = 0.f;
         const float ve = shdn(vw);
         const int f = r - 3;
-        float hw_3 = 0.f, hraw = 0.f, rr1 = 0.f, pct1 = 0.f, ev1 = 0.f, ql1 = 0.f;
+        float hw_3 = 0.f, hres = 0.f, clampv = 0.f, rr1 = 0.f, pct1 = 0.f, ev1 = 0.f, ql1 = 0.f;
         if (m3) {
             const float ho = h3;
             const bool hi = ho >= gt_ev;
@@ -330,13 +345,30 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
             ql1 = nsrc ? source_at(f, true) : 0.f;
             rr1 = storm ? storm_rate(f, on1, sx1, sy1) : u_rr1;
             if (RAINW) rr1 = rr1 * Win[f * pitch + gj];
-            hraw = ho - dt2 * ((us - un) * rdx + (ve - vw) * rdy - ql1 - rr1 * pct1 + ev1);
-            hw_3 = fmaxf(hraw, 0.f);
+            // compensated depth: the state is the FP32 pair h + remainder, and the
+            // update is added with two error-free sums, so that changes below half
+            // an ulp of h (light rain on deep water) accumulate in the remainder
+            // instead of being rounded away, which would leave the FP32 state
+            // behind its FP64 budget.  The fast two-sum is exact here: an update
+            // larger than the depth either drains the cell (clamped below) or
+            // fills it from 0, and the remainder is below an ulp of the depth.
+            const float d = __fmul_rn(-dt2, (us - un) * rdx + (ve - vw) * rdy - ql1 - rr1 * pct1 + ev1);
+            float s, e, hn, rn;
+            fast_two_sum(ho, d, s, e);
+            fast_two_sum(s, __fadd_rn(res3, e), hn, rn);
+            if (hn < 0.f) {  // fmax(h, 0) (cu:657) of the pair
+                clampv = -__fadd_rn(hn, rn);
+                hn = 0.f;
+                rn = 0.f;
+            }
+            hw_3 = hn;
+            hres = rn;
         }
         const float hwW = shup(hw_3);
         if (out_col && f >= R0) {  // f <= R1 - 1 always
             const int gp = f * pitch + gj;
             Hout[gp] = hw_3;
+            Rout[gp] = hres;
             Uout[gp] = un;
             Vout[gp] = vw;
             if (f == rows - 1) {  // south face, and the depth copy below the last row
@@ -348,7 +380,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
                 A.rain += rr1 * pct1;
                 A.src += ql1;
                 A.ev += ev1;
-                if (hraw < 0.f) A.clamp -= hraw;
+                A.clamp += clampv;
                 // CFL bound of the new state on the owned faces (extension)
                 if (m4) {
                     const float hm = 0.50f * (hw_3 + hw_4);
