@@ -36,6 +36,7 @@ struct HostScenario {
     bool raster = false;
     void *block = nullptr;
     size_t bytes = 0;
+    double volume0 = 0.0;  // water of the admitted state [m^3]
     ScenarioDev dev{};
 };
 
@@ -230,6 +231,27 @@ int sw2d_batch_destroy(sw2d_batch *b) {
     return SW2D_OK;
 }
 
+namespace {
+// Water on the active cells of buffer `buf` of a scenario [m^3]: deterministic
+// FP64 partials on the device (depth + remainder), Kahan-summed here; waits.
+int scenario_volume(sw2d_batch *b, const HostScenario &h, int buf, double *vol) {
+    BCK(b, launch_volume(h.dev.h[buf], h.dev.hr[buf], h.dev.mask, h.cfg.rows, h.cfg.cols, h.pitch, b->d_partial,
+                         kVolumeBlocks, b->stream));
+    BCK(b, cudaMemcpyAsync(b->h_partial, b->d_partial, kVolumeBlocks * sizeof(double), cudaMemcpyDeviceToHost,
+                           b->stream));
+    BCK(b, cudaStreamSynchronize(b->stream));
+    double s = 0.0, c = 0.0;
+    for (int q = 0; q < kVolumeBlocks; q++) {
+        const double y = b->h_partial[q] - c;
+        const double t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    *vol = s * h.cfg.dx * h.cfg.dy;
+    return SW2D_OK;
+}
+}  // namespace
+
 int sw2d_batch_add(sw2d_batch *b, const sw2d_config *cfg, const double *z, const double *manning,
                    const double *depth, int32_t rain_kind, const double *rain, int32_t n_rain, double rain_dt,
                    double t_end, int32_t *id) {
@@ -366,6 +388,8 @@ int sw2d_batch_add(sw2d_batch *b, const sw2d_config *cfg, const double *z, const
     d.nman = n_dev;
     d.mask = m_dev;
     d.clk = clk;
+    int vrc = scenario_volume(b, h, 0, &h.volume0);  // the admitted state, as the FP32 planes hold it
+    if (vrc) return vrc;
     d.status = b->d_status + slot;
     d.tiles_w = h.tiles_w;
     d.strip_h = h.strip_h;
@@ -480,6 +504,7 @@ int sw2d_batch_get_field(sw2d_batch *b, int32_t id, int32_t field, double *out) 
     return SW2D_OK;
 }
 
+
 int sw2d_batch_get_budget(sw2d_batch *b, int32_t id, sw2d_budget *out) {
     if (!b || !out || id < 0 || id >= (int)b->scen.size() || !b->scen[id].active)
         return bfail(b, SW2D_ERR_INVALID_ARG, "bad scenario id");
@@ -487,26 +512,17 @@ int sw2d_batch_get_budget(sw2d_batch *b, int32_t id, sw2d_budget *out) {
     int rc = read_current_clock(b, h);
     if (rc) return rc;
     const Clock k = *b->h_clk;
-    BCK(b, launch_volume(h.dev.h[k.buf], h.dev.hr[k.buf], h.dev.mask, h.cfg.rows, h.cfg.cols, h.pitch, b->d_partial, kVolumeBlocks,
-                         b->stream));
-    BCK(b, cudaMemcpyAsync(b->h_partial, b->d_partial, kVolumeBlocks * sizeof(double), cudaMemcpyDeviceToHost,
-                           b->stream));
-    BCK(b, cudaStreamSynchronize(b->stream));
-    double s = 0.0, c = 0.0;
-    for (int q = 0; q < kVolumeBlocks; q++) {
-        const double y = b->h_partial[q] - c;
-        const double t = s + y;
-        c = (t - s) - y;
-        s = t;
-    }
+    double vol = 0.0;
+    rc = scenario_volume(b, h, k.buf, &vol);
+    if (rc) return rc;
     double tot[B_N];
     for (int q = 0; q < B_N; q++) tot[q] = k.tot_s[q] + (k.step[q] - k.tot_c[q]);
     std::memset(out, 0, sizeof(*out));
     out->t = k.t;
     out->dt = k.dt;
     std::memcpy(&out->cmax, &k.cmax_bits, sizeof(double));
-    out->volume = s * h.cfg.dx * h.cfg.dy;
-    out->volume0 = 0.0;
+    out->volume = vol;
+    out->volume0 = h.volume0;
     out->rain_in = tot[B_RAIN];
     out->source_in = tot[B_SRC];
     out->evap_out = tot[B_EV];
