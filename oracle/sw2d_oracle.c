@@ -118,14 +118,19 @@ static void kadd(kahan *k, double v) {
  * the storm forcing needs exp().  Library pow/exp differ by ulps between
  * glibc and CUDA, and near the wet/dry threshold such ulps grow into
  * visible depth differences.  The oracle and the FP64 device path therefore
- * both use this routine, built only from IEEE-exact + - * / (no FMA), so the
- * two give identical bits:
- *   log: x = m 2^e, m in [1/sqrt2, sqrt2), log m = 2 atanh(s) with
- *        s = (m-1)/(m+1) (|s| <= 0.1716) summed to s^21/21 (Horner);
- *   exp: Cody-Waite reduction y = k ln2 + r, |r| <= ln2/2, Taylor series
- *        of e^r to r^13/13!, scaled by 2^k built from its bit pattern;
- *   ln2 split into a 21-bit head (exact k*LN2_HI) and a tail.
- * Both are accurate to a few ulps (checked against glibc pow in tests). */
+ * both use these routines, built only from IEEE-exact + - * / (no FMA), so
+ * the two give identical bits.
+ *
+ * Table-driven forms (what the update calls):
+ *   log: x = m 2^e with m in [1,2); the top 7 bits of m pick c = 1 + k/128;
+ *        r = (m - c) * (1/c) (m - c exact), r in [0, 1/128); ln(1+r) by its
+ *        series to r^8/8 (truncation < 2e-20); ln x = e ln2 + ln c + ln(1+r);
+ *   exp: y = n ln2/64 + r with n = round(64 y/ln2), |r| <= ln2/128; e^r by
+ *        its series to r^6/6! (truncation < 2e-20); e^y = 2^(n>>6) 2^((n&63)/64) e^r;
+ *   ln2 and ln2/64 split into a 21-bit head (exact multiples) and a tail.
+ * The tables 1/c, ln c and 2^(j/64) are built once from the series forms
+ * below (log: atanh series on [1/sqrt2, sqrt2) to s^21/21; exp: Cody-Waite
+ * by ln2 and Taylor to r^13/13!), the same way on the GPU. */
 #define ORC_LN2_HI 0x1.62e42p-1
 #define ORC_LN2_LO 0x1.fdf473de6af28p-22
 #define ORC_INV_LN2 0x1.71547652b82fep+0
@@ -133,7 +138,7 @@ static void kadd(kahan *k, double v) {
 static double bits2d(uint64_t b) { double d; memcpy(&d, &b, 8); return d; }
 static uint64_t d2bits(double d) { uint64_t b; memcpy(&b, &d, 8); return b; }
 
-double orc_log(double x) {
+static double log_series(double x) {
     uint64_t b = d2bits(x);
     int e = (int)((b >> 52) & 0x7ff) - 1023;
     double m = bits2d((b & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL);
@@ -159,9 +164,7 @@ double orc_log(double x) {
     return ef * ORC_LN2_HI + (ef * ORC_LN2_LO + lm);
 }
 
-double orc_exp(double y) {
-    if (y < -700.0) return 0.0;
-    if (y > 700.0) return HUGE_VAL;
+static double exp_series(double y) {
     double kf = floor(y * ORC_INV_LN2 + 0.5);
     double r = (y - kf * ORC_LN2_HI) - kf * ORC_LN2_LO;
     double p = 1.0 / 6227020800.0;
@@ -180,6 +183,55 @@ double orc_exp(double y) {
     p = p * r + 1.0;
     int k = (int)kf;
     return p * bits2d((uint64_t)(k + 1023) << 52);
+}
+
+static double T_INV[128], T_LOGC[128], T_EXP2J[64];
+
+__attribute__((constructor)) static void init_tables(void) {
+    for (int k = 0; k < 128; k++) {
+        double c = 1.0 + (double)k * 0.0078125;
+        T_INV[k] = 1.0 / c;
+        T_LOGC[k] = log_series(c);
+    }
+    for (int j = 0; j < 64; j++)
+        T_EXP2J[j] = exp_series((double)j * (ORC_LN2_HI / 64.0) + (double)j * (ORC_LN2_LO / 64.0));
+}
+
+double orc_log(double x) {
+    uint64_t b = d2bits(x);
+    int e = (int)((b >> 52) & 0x7ff) - 1023;
+    int k = (int)((b >> 45) & 127);
+    double m = bits2d((b & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL);
+    double c = 1.0 + (double)k * 0.0078125;
+    double r = (m - c) * T_INV[k];
+    double p = -1.0 / 8.0;
+    p = p * r + 1.0 / 7.0;
+    p = p * r - 1.0 / 6.0;
+    p = p * r + 1.0 / 5.0;
+    p = p * r - 1.0 / 4.0;
+    p = p * r + 1.0 / 3.0;
+    p = p * r - 0.5;
+    p = p * r + 1.0;
+    double lr = p * r;
+    double ef = (double)e;
+    return ef * ORC_LN2_HI + (ef * ORC_LN2_LO + (T_LOGC[k] + lr));
+}
+
+double orc_exp(double y) {
+    if (y < -700.0) return 0.0;
+    if (y > 700.0) return HUGE_VAL;
+    double nf = floor(y * (64.0 * ORC_INV_LN2) + 0.5);
+    double r = (y - nf * (ORC_LN2_HI / 64.0)) - nf * (ORC_LN2_LO / 64.0);
+    double p = 1.0 / 720.0;
+    p = p * r + 1.0 / 120.0;
+    p = p * r + 1.0 / 24.0;
+    p = p * r + 1.0 / 6.0;
+    p = p * r + 0.5;
+    p = p * r + 1.0;
+    p = p * r + 1.0;
+    int n = (int)nf;
+    int j = n & 63, q = (n - j) / 64;  /* n = 64 q + j, 0 <= j < 64 */
+    return (p * T_EXP2J[j]) * bits2d((uint64_t)(q + 1023) << 52);
 }
 
 /* hm^1.3333330 of the friction term (cu:195, cu:312), for hm > th > 0 */

@@ -7,7 +7,18 @@
 
 namespace sw2d {
 
+// Fills this translation unit's tables of the deterministic log/exp (on the
+// legacy stream, waited for: the handles' own streams do not order with it).
+cudaError_t init_det_tables() {
+    det_tables_kernel<<<1, 128>>>();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(0);
+}
+
 cudaError_t prepare_step(int th, int tw, double) {
+    const cudaError_t e = init_det_tables();
+    if (e != cudaSuccess) return e;
     if (th == 16 && tw == 32) return detail::step_prepare<double, 16, 32, 256>();
     if (th == 8 && tw == 32) return detail::step_prepare<double, 8, 32, 128>();
     return cudaErrorInvalidValue;

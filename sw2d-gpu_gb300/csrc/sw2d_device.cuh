@@ -382,14 +382,18 @@ __device__ inline void finish_cta(const Clock &ci, Clock &co, Clock &cn, const P
 }
 
 // ---------------------------------------------------------------------------
-// deterministic FP64 log / exp / power.  Same algorithm and operation order
-// as the oracle's (log: atanh series on m in [1/sqrt2, sqrt2); exp:
-// Cody-Waite reduction by ln2 split into a 21-bit head and a tail, Taylor
-// series to r^13/13!, scaling by 2^k from its bit pattern), compiled without
-// FMA contraction, so the FP64 path and the oracle agree to the bit where
-// the reference uses pow (cu:195, cu:312).
+// deterministic FP64 log / exp / power.  Same algorithm, operation order and
+// tables as the oracle's, compiled without FMA contraction, so the FP64 path
+// and the oracle agree to the bit where the reference uses pow (cu:195,
+// cu:312).  The update uses the table-driven forms: log with 1/c and ln c for
+// c = 1 + k/128 (k = the top 7 bits of the mantissa) and the series of
+// ln(1+r) to r^8/8; exp with a reduction by ln2/64, the series of e^r to
+// r^6/6! and 2^(j/64).  The tables are built by det_tables_kernel from the
+// series forms (log: atanh series on [1/sqrt2, sqrt2) to s^21/21; exp:
+// Cody-Waite by ln2, Taylor to r^13/13!) in each translation unit that uses
+// them (init_det_tables).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double det_log(double x) {
+__device__ __forceinline__ double det_log_series(double x) {
     const long long b = __double_as_longlong(x);
     int e = (int)((b >> 52) & 0x7ff) - 1023;
     double m = __longlong_as_double((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
@@ -415,9 +419,7 @@ __device__ __forceinline__ double det_log(double x) {
     return ef * 0x1.62e42p-1 + (ef * 0x1.fdf473de6af28p-22 + lm);
 }
 
-__device__ __forceinline__ double det_exp(double y) {
-    if (y < -700.0) return 0.0;
-    if (y > 700.0) return __longlong_as_double(0x7ff0000000000000LL);
+__device__ __forceinline__ double det_exp_series(double y) {
     const double kf = floor(y * 0x1.71547652b82fep+0 + 0.5);
     const double r = (y - kf * 0x1.62e42p-1) - kf * 0x1.fdf473de6af28p-22;
     double p = 1.0 / 6227020800.0;
@@ -436,6 +438,58 @@ __device__ __forceinline__ double det_exp(double y) {
     p = p * r + 1.0;
     const int k = (int)kf;
     return p * __longlong_as_double((long long)(k + 1023) << 52);
+}
+
+// [0,128): 1/c_k, [128,256): ln c_k, [256,320): 2^(j/64); one copy per
+// translation unit, filled by det_tables_kernel before the first use
+static __device__ double g_det_tab[320];
+
+static __global__ void det_tables_kernel() {
+    const int t = threadIdx.x;
+    if (t < 128) {
+        const double c = 1.0 + (double)t * 0.0078125;
+        g_det_tab[t] = 1.0 / c;
+        g_det_tab[128 + t] = det_log_series(c);
+    }
+    if (t < 64)
+        g_det_tab[256 + t] = det_exp_series((double)t * (0x1.62e42p-1 / 64.0) + (double)t * (0x1.fdf473de6af28p-22 / 64.0));
+}
+
+__device__ __forceinline__ double det_log(double x) {
+    const long long b = __double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023;
+    const int k = (int)((b >> 45) & 127);
+    const double m = __longlong_as_double((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+    const double c = 1.0 + (double)k * 0.0078125;
+    const double r = (m - c) * __ldg(&g_det_tab[k]);
+    double p = -1.0 / 8.0;
+    p = p * r + 1.0 / 7.0;
+    p = p * r - 1.0 / 6.0;
+    p = p * r + 1.0 / 5.0;
+    p = p * r - 1.0 / 4.0;
+    p = p * r + 1.0 / 3.0;
+    p = p * r - 0.5;
+    p = p * r + 1.0;
+    const double lr = p * r;
+    const double ef = (double)e;
+    return ef * 0x1.62e42p-1 + (ef * 0x1.fdf473de6af28p-22 + (__ldg(&g_det_tab[128 + k]) + lr));
+}
+
+__device__ __forceinline__ double det_exp(double y) {
+    if (y < -700.0) return 0.0;
+    if (y > 700.0) return __longlong_as_double(0x7ff0000000000000LL);
+    const double nf = floor(y * (64.0 * 0x1.71547652b82fep+0) + 0.5);
+    const double r = (y - nf * (0x1.62e42p-1 / 64.0)) - nf * (0x1.fdf473de6af28p-22 / 64.0);
+    double p = 1.0 / 720.0;
+    p = p * r + 1.0 / 120.0;
+    p = p * r + 1.0 / 24.0;
+    p = p * r + 1.0 / 6.0;
+    p = p * r + 0.5;
+    p = p * r + 1.0;
+    p = p * r + 1.0;
+    const int n = (int)nf;
+    const int j = n & 63, q = (n - j) / 64;  // n = 64 q + j, 0 <= j < 64
+    return (p * __ldg(&g_det_tab[256 + j])) * __longlong_as_double((long long)(q + 1023) << 52);
 }
 
 // ---------------------------------------------------------------------------
