@@ -1,5 +1,5 @@
 // sw2d_stream_unit.cuh -- one warp's work in the FP32 streaming scheme: a
-// strip of rows of a 32-column window of one scenario (25 output columns).
+// strip of rows of a 32-column window of one scenario (26 output columns).
 //
 // Shared by the single-scenario streaming kernel (sw2d_stream.cuh) and the
 // batched kernel (sw2d_batch.cuh); the arithmetic is that of step_kernel in
@@ -11,7 +11,17 @@
 
 namespace sw2d {
 
-constexpr int kStreamHL = 4;                            // west halo lanes (3 + CFL ring)
+// Halo lanes: lanes whose results are incomplete because a neighbour they
+// need lies outside the window (the shuffles return a lane's own value at the
+// window's edges).  West: each lane loads its west neighbour's depth instead
+// of shuffling it, so the face velocities of lane 0 are exact; its discharges
+// are not (they need lane -1's velocities), lane 1's are; so the dry-cell
+// flags are exact from lane 1, the final depths from lane 2 (the west face
+// tests the west cell's flag) and the CFL bounds of the y-faces, which take
+// the west cell's final depth, from lane 3.  East, by the same chain: lane
+// 31's discharges, lane 30's provisional depth and lane 29's final depth (its
+// east face tests lane 30's flag) are incomplete.
+constexpr int kStreamHL = 3;                            // west halo lanes
 constexpr int kStreamHR = 3;                            // east halo lanes
 constexpr int kStreamOut = 32 - kStreamHL - kStreamHR;  // output columns per warp
 constexpr int kStreamMaxSrc = 16;                       // point sources per warp strip
@@ -215,12 +225,13 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     // row loads: rows R0-4 .. R1+2 and columns gj0 .. gj0+31 all lie inside
     // the zero frame around the domain, whose zeros are the inactive-cell and
     // wall values, so no load needs a bounds test
-    float p_h, p_dzx, p_dzy, p_n, p_um, p_vn, p_res;
+    float p_h, p_hw, p_dzx, p_dzy, p_n, p_um, p_vn, p_res;
     unsigned p_m;
     int gp = (R0 - 4) * pitch + gj;  // element offset of the next row to read (fields fit 32-bit offsets)
     int lrow = R0 - 4;  // row of the next load
     auto load_row = [&]() {
         p_h = Hin[gp];
+        p_hw = Hin[gp - 1];  // the west neighbour's depth, exact on lane 0 too
         p_res = lrow >= 3 ? Rin[gp - 3 * pitch] : 0.f;  // remainder of row lrow-3, used with this row
         lrow++;
         p_dzx = DZX[gp];
@@ -248,14 +259,13 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     load_row();
 #pragma unroll UNR
     for (int r = r_first; r < r_last; r++) {
-        const float h0 = p_h, dzx0 = p_dzx, dzy0 = p_dzy, n0 = p_n, um0 = p_um, vn0 = p_vn;
+        const float h0 = p_h, hL0 = p_hw, dzx0 = p_dzx, dzy0 = p_dzy, n0 = p_n, um0 = p_um, vn0 = p_vn;
         const float res3 = p_res;  // depth remainder of row r-3
         mb = (mb << 1) | p_m;
         const unsigned mL0 = __shfl_up_sync(0xffffffffu, p_m, 1);
         mLb = (mLb << 1) | mL0;
         if (r + 1 < r_last) load_row();  // prefetch the next row
 
-        const float hL0 = shup(h0);
         const float nL0 = raster ? shup(n0) : manning;
         // ---- row r: face velocities (cu:363-453) ----
         const float hnf = 0.50f * (h0 + hL0);
@@ -393,7 +403,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
                     if (hn >= ge_th) A.cm = fmaxf(A.cm, wave_speed(vw, hn));
                 }
             }
-            if (!isfinite(hw_3) || !isfinite(un) || !isfinite(vw)) A.bad = true;
+            if (!isfinite(hw_3 + un + vw)) A.bad = true;  // a NaN or an infinity in any of the three
         }
 
         // ---- advance the rings ----

@@ -115,7 +115,8 @@ def test_stream_variants_agree(sw2d_mod, variant):
     assert b0["t"] == b1["t"]
 
 
-@pytest.mark.parametrize("shape", [(1, 1), (1, 9), (9, 1), (17, 33), (33, 17), (3, 65), (40, 26), (5, 50)])
+@pytest.mark.parametrize("shape", [(1, 1), (1, 9), (9, 1), (17, 33), (33, 17), (3, 65), (40, 26), (5, 50), (7, 57),
+                                   (6, 113)])
 def test_stream_ragged_grids_vs_oracle(oracle_mod, sw2d_mod, shape):
     rows, cols = shape
     rng = np.random.default_rng(rows * 100 + cols)
