@@ -9,12 +9,13 @@ namespace sw2d {
 
 // Every device field is a pitched array with a zero frame around the domain:
 // kGhostTop rows above row 0, kGhostBottom rows below the south face row,
-// kGhostLeft columns left of column 0 and at least 27 right of the east wall.
+// kGhostLeft columns left of column 0 and at least 30 right of the east wall
+// (the streaming kernel's last window reads 29 columns past it).
 // Kernel pointers point at cell (0,0); the FP32 streaming kernel reads the
 // frame instead of testing bounds (zero = inactive cell / wall, exactly the
 // values the bounds tests would substitute).
 constexpr int kGhostTop = 4, kGhostBottom = 4, kGhostLeft = 4;
-inline int pitch_for(int cols) { return ((cols + 32 + 31) / 32) * 32; }
+inline int pitch_for(int cols) { return ((cols + 34 + 31) / 32) * 32; }
 inline size_t plane_for(int rows, int pitch) { return (size_t)(kGhostTop + rows + 1 + kGhostBottom) * pitch; }
 inline size_t origin_for(int pitch) { return (size_t)kGhostTop * pitch + kGhostLeft; }
 // Kernels index a field, frame included, with 32-bit element offsets.

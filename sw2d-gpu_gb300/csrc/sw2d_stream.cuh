@@ -4,10 +4,11 @@
 // SW2D-GPU_linux/src/SW2D-GPU.cu:1256-1336), organised for the FP32 path's
 // instruction budget instead of for FP64 reuse:
 //
-//   * one warp owns 32 adjacent columns -- 26 output columns plus 3 halo
-//     columns on each side, the lateral dependency radius of one iteration
-//     (the west one shortened by loading each lane's west depth) -- and
-//     marches down a strip of rows (stream_unit in sw2d_stream_unit.cuh);
+//   * one warp owns 32 adjacent columns -- 27 output columns plus 3 halo
+//     columns on the west and 2 on the east, the lateral dependency radius
+//     of one iteration (shortened by loading the neighbours' depths and
+//     discharges at the window's edges) -- and marches down a strip of rows
+//     (stream_unit in sw2d_stream_unit.cuh);
 //   * each row read from HBM (h, z, n, mask, um, vn; one coalesced line per
 //     field and warp) feeds a 3-row register pipeline
 //         row r    : face depths and velocities uu1/vv1        (cu:363-453)

@@ -1,5 +1,5 @@
 // sw2d_stream_unit.cuh -- one warp's work in the FP32 streaming scheme: a
-// strip of rows of a 32-column window of one scenario (26 output columns).
+// strip of rows of a 32-column window of one scenario (27 output columns).
 //
 // Shared by the single-scenario streaming kernel (sw2d_stream.cuh) and the
 // batched kernel (sw2d_batch.cuh); the arithmetic is that of step_kernel in
@@ -18,11 +18,16 @@ namespace sw2d {
 // are not (they need lane -1's velocities), lane 1's are; so the dry-cell
 // flags are exact from lane 1, the final depths from lane 2 (the west face
 // tests the west cell's flag) and the CFL bounds of the y-faces, which take
-// the west cell's final depth, from lane 3.  East, by the same chain: lane
-// 31's discharges, lane 30's provisional depth and lane 29's final depth (its
-// east face tests lane 30's flag) are incomplete.
+// the west cell's final depth, from lane 3.  East: each lane loads its east
+// neighbour's depth and discharges and computes that lane's y-face velocity
+// itself, so the discharges of lane 31 are exact too; its provisional depth
+// is not (it needs lane 32's y-face discharge), so the dry-cell flags are
+// exact up to lane 30 and the final depths up to lane 29 (the east face
+// tests the east cell's flag).  Loading a neighbour's values in place of a
+// shuffle costs the same issue slot; recomputing lane -1's velocities as
+// well (a 2-lane west halo) cost more than the lane saved.
 constexpr int kStreamHL = 3;                            // west halo lanes
-constexpr int kStreamHR = 3;                            // east halo lanes
+constexpr int kStreamHR = 2;                            // east halo lanes
 constexpr int kStreamOut = 32 - kStreamHL - kStreamHR;  // output columns per warp
 constexpr int kStreamMaxSrc = 16;                       // point sources per warp strip
 
@@ -225,7 +230,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     // row loads: rows R0-4 .. R1+2 and columns gj0 .. gj0+31 all lie inside
     // the zero frame around the domain, whose zeros are the inactive-cell and
     // wall values, so no load needs a bounds test
-    float p_h, p_hw, p_dzx, p_dzy, p_n, p_um, p_vn, p_res;
+    float p_h, p_hw, p_hE, p_umE, p_vnE, p_dzx, p_dzy, p_n, p_um, p_vn, p_res;
     unsigned p_m;
     int gp = (R0 - 4) * pitch + gj;  // element offset of the next row to read (fields fit 32-bit offsets)
     int lrow = R0 - 4;  // row of the next load
@@ -240,6 +245,9 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         p_m = (unsigned)Min[gp];
         p_um = Uin[gp];
         p_vn = Vin[gp];
+        p_hE = Hin[gp + 1];  // the east neighbour's depth and discharges
+        p_umE = Uin[gp + 1];
+        p_vnE = Vin[gp + 1];
         gp += pitch;
     };
 
@@ -249,7 +257,8 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     float n1 = manning, n2 = manning, nL1 = manning;
     float um1 = 0.f, um2 = 0.f, vn1 = 0.f, vn2 = 0.f;
     float uu_1 = 0.f, uu_2 = 0.f, uuL_1 = 0.f;
-    float vv_1 = 0.f, vv_2 = 0.f, vvR_2 = 0.f;
+    float vv_1 = 0.f, vv_2 = 0.f, vvR_1 = 0.f, vvR_2 = 0.f;
+    float umE1 = 0.f, vnE1 = 0.f;  // the east neighbour's discharges of row r-1
     float rum_2 = 0.f, rum_3 = 0.f, rvn_2 = 0.f, rvn_3 = 0.f;
     float hw_4 = 0.f;
     unsigned mb = 0u, mLb = 0u;  // bit k: active mask of row r-k (own / west column)
@@ -259,6 +268,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     load_row();
 #pragma unroll UNR
     for (int r = r_first; r < r_last; r++) {
+        const float hE0 = p_hE, umE0 = p_umE, vnE0 = p_vnE;
         const float h0 = p_h, hL0 = p_hw, dzx0 = p_dzx, dzy0 = p_dzy, n0 = p_n, um0 = p_um, vn0 = p_vn;
         const float res3 = p_res;  // depth remainder of row r-3
         mb = (mb << 1) | p_m;
@@ -273,12 +283,14 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         const float hmf = 0.50f * (h0 + h1);
         const float uu_0 = (hmf >= ge_th) ? um0 / hmf : 0.0f;
         const float uuL_0 = shup(uu_0);
-        const float vvR_1 = shdn(vv_1);
+        // the east neighbour's y-face velocity, as that lane computes it
+        const float hnfE = 0.50f * (hE0 + h0);
+        const float vvE_0 = (hnfE >= ge_th) ? vnE0 / hnfE : 0.0f;
 
         // ---- row r-1: new face discharges (cu:98-354) ----
         const int i = r - 1;
-        const float umE = shdn(um1), umW = shup(um1);
-        const float vnE = shdn(vn1), vnW = shup(vn1);
+        const float umE = umE1, umW = shup(um1);
+        const float vnE = vnE1, vnW = shup(vn1);
         const float vvW = shup(vv_1);
         float rum_1 = 0.f;
         {
@@ -412,7 +424,8 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         n2 = n1; n1 = n0; nL1 = nL0;
         um2 = um1; um1 = um0; vn2 = vn1; vn1 = vn0;
         uu_2 = uu_1; uu_1 = uu_0; uuL_1 = uuL_0;
-        vv_2 = vv_1; vv_1 = vv_0; vvR_2 = vvR_1;
+        vv_2 = vv_1; vv_1 = vv_0; vvR_2 = vvR_1; vvR_1 = vvE_0;
+        umE1 = umE0; vnE1 = vnE0;
         rum_3 = rum_2; rum_2 = rum_1; rvn_3 = rvn_2; rvn_2 = rvn_1;
         hw_4 = hw_3;
     }

@@ -22,7 +22,7 @@ import numpy as np
 STRIPS = (16, 24, 32, 48, 64, 96, 128)
 VARIANTS = (0, 1, 2, 3, 4, 5)
 CHUNKS = (12, 24, 48, 96)
-OUT_COLS = 26            # output columns of one streaming warp
+OUT_COLS = 27            # output columns of one streaming warp
 RESIDENT_WARPS_PER_SM = (16, 20, 24)  # resident warps per SM of the kernel builds
 
 

@@ -75,5 +75,5 @@ def test_describe_names_the_kernel_run(sw2d_mod):
     assert d.startswith("stream_step_kernel<") and "strip_h=" in d
     strip = int(d.split("strip_h=")[1].split()[0])
     units = int(d.split("units=")[1].split()[0])
-    assert units == -(-200 // 26) * -(-300 // strip)  # column tiles x strips
+    assert units == -(-200 // 27) * -(-300 // strip)  # column tiles x strips
     g.close()
