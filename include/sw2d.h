@@ -54,7 +54,7 @@ enum { SW2D_PREC_F64 = 0, SW2D_PREC_F32 = 1 };
 enum { SW2D_DT_FIXED = 0, SW2D_DT_CFL = 1 };
 
 /* Step kernels.  TILE: one CTA per 2-D tile staged in shared memory (the
- * FP64 path).  STREAM: one warp per 25-column strip marching down the rows
+ * FP64 path).  STREAM: one warp per 27-column strip marching down the rows
  * with a register pipeline (FP32 only).  AUTO: TILE for FP64, STREAM for FP32. */
 enum { SW2D_KERNEL_AUTO = 0, SW2D_KERNEL_TILE = 1, SW2D_KERNEL_STREAM = 2 };
 
