@@ -214,7 +214,7 @@ int sw2d_get_stream(sw2d_handle *h, void **stream);
 int sw2d_launch_count(sw2d_handle *h, int64_t *launches);
 
 /* One line naming the step kernel build and the decomposition the handle
- * runs, e.g. "stream_step_kernel<2,10,2> strip_h=52 units=3040 ctas=1520"
+ * runs, e.g. "stream_step_kernel<2,10,2> forcing=uniform strip_h=52 units=3040 ctas=1520"
  * (written NUL-terminated, truncated to `n` bytes).  No reference
  * counterpart: the reference's launch shape is fixed at cu:1222-1235. */
 int sw2d_describe(const sw2d_handle *h, char *buf, int32_t n);

@@ -51,12 +51,16 @@ int stream_warps(int variant) {
 cudaError_t prepare_stream_step(int variant) {
 #define SW2D_P(id, nw, mb, un)                                                                            \
     if (variant == id) {                                                                               \
-        cudaError_t e = cudaFuncSetAttribute(stream_step_kernel<nw, mb, un, false>,                    \
-                                             cudaFuncAttributePreferredSharedMemoryCarveout,           \
-                                             kStreamCarveoutPercent);                                  \
-        if (e != cudaSuccess) return e;                                                                \
-        return cudaFuncSetAttribute(stream_step_kernel<nw, mb, un, true>,                              \
-                                    cudaFuncAttributePreferredSharedMemoryCarveout, kStreamCarveoutPercent); \
+        const void *k[4] = {(const void *)stream_step_kernel<nw, mb, un, false, false>,                \
+                            (const void *)stream_step_kernel<nw, mb, un, false, true>,                 \
+                            (const void *)stream_step_kernel<nw, mb, un, true, false>,                 \
+                            (const void *)stream_step_kernel<nw, mb, un, true, true>};                 \
+        for (const void *f : k) {                                                                      \
+            cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout,   \
+                                                 kStreamCarveoutPercent);                             \
+            if (e != cudaSuccess) return e;                                                            \
+        }                                                                                              \
+        return cudaSuccess;                                                                            \
     }
     SW2D_STREAM_VARIANTS(SW2D_P)
 #undef SW2D_P
@@ -75,7 +79,7 @@ int stream_ctas_per_sm(int variant) {
     int n = 0;
 #define SW2D_O(id, nw, mb, un)                                                                           \
     if (variant == id &&                                                                                 \
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stream_step_kernel<nw, mb, un, false>, nw * 32, 0) != \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stream_step_kernel<nw, mb, un, false, false>, nw * 32, 0) != \
             cudaSuccess)                                                                                 \
         n = 0;
     SW2D_STREAM_VARIANTS(SW2D_O)
@@ -91,13 +95,19 @@ cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_
     sh.strip_h = strip_h;
     sh.units = units;
     sh.pad = 0;
-#define SW2D_L(id, nw, mb, un)                                                                          \
-    if (variant == id) {                                                                              \
-        if (S.rainw)                                                                                  \
-            stream_step_kernel<nw, mb, un, true><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh);  \
-        else                                                                                          \
-            stream_step_kernel<nw, mb, un, false><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh); \
-        return cudaGetLastError();                                                                    \
+    // the general build carries the moving storm and the point sources
+    const bool gen = F.rain_kind == RAIN_STORM || G.n_src > 0;
+#define SW2D_L(id, nw, mb, un)                                                                             \
+    if (variant == id) {                                                                                 \
+        if (S.rainw && gen)                                                                              \
+            stream_step_kernel<nw, mb, un, true, true><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh);   \
+        else if (S.rainw)                                                                                \
+            stream_step_kernel<nw, mb, un, true, false><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh);  \
+        else if (gen)                                                                                    \
+            stream_step_kernel<nw, mb, un, false, true><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh);  \
+        else                                                                                             \
+            stream_step_kernel<nw, mb, un, false, false><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh); \
+        return cudaGetLastError();                                                                       \
     }
     SW2D_STREAM_VARIANTS(SW2D_L)
 #undef SW2D_L

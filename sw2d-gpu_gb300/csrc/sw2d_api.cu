@@ -898,9 +898,14 @@ int sw2d_launch_count(sw2d_handle *h, int64_t *launches) {
 
 int sw2d_describe(const sw2d_handle *h, char *buf, int32_t n) {
     if (!h || !buf || n <= 0) return SW2D_ERR_INVALID_ARG;
-    if (h->stream_kernel)
-        snprintf(buf, (size_t)n, "%s strip_h=%d units=%d ctas=%d", stream_variant_name(h->variant), h->strip_h,
+    if (h->stream_kernel) {
+        // the forcing build the launcher picks (step_f32.cu): storm and point
+        // sources, per-cell rain factors, or neither
+        const bool gen = h->F.rain_kind == RAIN_STORM || h->G.n_src > 0;
+        snprintf(buf, (size_t)n, "%s forcing=%s%s strip_h=%d units=%d ctas=%d", stream_variant_name(h->variant),
+                 gen ? "storm/sources" : "uniform", h->use_rainw ? "+rain_weights" : "", h->strip_h,
                  h->stream_units, h->nblocks);
+    }
     else
         snprintf(buf, (size_t)n, "step_kernel<%s,%d,%d> ctas=%d", is_f64(h) ? "double" : "float", h->tile_h,
                  h->tile_w, h->nblocks);

@@ -119,7 +119,9 @@ __global__ void __launch_bounds__(NWARP * 32, MINB) batch_step_kernel(const Batc
             A.rain = A.src = A.ev = A.out = A.clamp = A.cm = 0.f;
             A.bad = A.too_many_sources = false;
             const int ct = ue.y % S.tiles_w, rs = ue.y / S.tiles_w;
-            stream_unit<1, false>(V, ct, rs, S.strip_h, lane, s_sr[wid], s_sc[wid], s_q0[wid], s_q1[wid], A);
+            // batched scenarios take neither a storm nor point sources nor rain
+            // factors (sw2d_batch_add accepts none), so the uniform-forcing unit
+            stream_unit<1, false, false>(V, ct, rs, S.strip_h, lane, s_sr[wid], s_sc[wid], s_q0[wid], s_q1[wid], A);
             warp_reduce_acc(A);
             if (lane == 0) {
                 const double area = S.G.dx * S.G.dy, scale = ci.plan.d.dt2 * area;

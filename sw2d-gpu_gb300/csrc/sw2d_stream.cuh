@@ -36,7 +36,9 @@ struct StreamShape {
     int pad;
 };
 
-template <int NWARP, int MINB, int UNR, bool RAINW>
+// RAINW: per-cell rain factors; GEN: moving storm and point sources (the
+// launcher picks the build from the handle's forcing).
+template <int NWARP, int MINB, int UNR, bool RAINW, bool GEN>
 __global__ void __launch_bounds__(NWARP * 32, MINB)
     stream_step_kernel(const GridDesc G, const ForcingDesc F, const StateBufs<float> S, const Thr<float> T,
                        Clock *__restrict__ clk, const Control *__restrict__ ctl, const int slot,
@@ -94,7 +96,7 @@ __global__ void __launch_bounds__(NWARP * 32, MINB)
         V.t1 = ci.plan.t1;
         V.dx = G.dx;
         V.dy = G.dy;
-        stream_unit<UNR, RAINW>(V, unit % SH.tiles_w, unit / SH.tiles_w, SH.strip_h, lane, s_sr[wid], s_sc[wid],
+        stream_unit<UNR, RAINW, GEN>(V, unit % SH.tiles_w, unit / SH.tiles_w, SH.strip_h, lane, s_sr[wid], s_sc[wid],
                              s_q0[wid], s_q1[wid], A);
     }
 

@@ -117,8 +117,11 @@ struct StreamAcc {
 // Advances column tile `ct`, row strip `rs` (strip height strip_h) of the
 // scenario in V.  s_sr/s_sc/s_q0/s_q1 are this warp's slots for local point
 // sources (kStreamMaxSrc each).  UNR is the unrolling of the row loop;
-// RAINW builds in the per-cell rain factors (V.Win), which the uniform-rain
-// build leaves out entirely (even unexecuted, that code slowed the loop).
+// RAINW builds in the per-cell rain factors (V.Win) and GEN the moving storm
+// and the point sources; the builds without them leave that code out
+// entirely, because even unexecuted it slowed the row loop (the rain factors
+// by 6-11 %, the storm and sources by 9 %, as instructions fetched past and
+// registers held, not as work).
 //
 // Domain edges need no tests of their own: the zero frame around every field
 // has mask 0, so the face tests on the two cells' masks already close the
@@ -129,7 +132,7 @@ struct StreamAcc {
 // face (cu:380-381), used by the open south edge.  Two rules of the
 // reference stay explicit: no cross advection u12 on column 0 (cu:178-180)
 // and no v11 on row 0 (cu:289-291).
-template <int UNR, bool RAINW>
+template <int UNR, bool RAINW, bool GEN>
 __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, const int rs, const int strip_h,
                                             const int lane, int *s_sr, int *s_sc, float *s_q0, float *s_q1,
                                             StreamAcc &A) {
@@ -138,7 +141,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     const float u_ev0 = wuni(V.LS.ev0), u_ev1 = wuni(V.LS.ev1), u_rr0 = wuni(V.LS.rr0), u_rr1 = wuni(V.LS.rr1);
     const float sx0 = wuni(V.LS.sx0), sy0 = wuni(V.LS.sy0), sx1 = wuni(V.LS.sx1), sy1 = wuni(V.LS.sy1);
     const float storm_amp = wuni(V.GS.storm_amp), storm_2s2 = wuni(V.GS.storm_2s2);
-    const int storm = wuni((int)V.storm), on0 = wuni((int)V.on0), on1 = wuni((int)V.on1);
+    const int storm = GEN ? wuni((int)V.storm) : 0, on0 = wuni((int)V.on0), on1 = wuni((int)V.on1);
     const float hdx = 0.5f * dt2dx, hdy = 0.5f * dt2dy;  // dt2/dx, dt2/dy times the halves of upw()
     const float dx = wuni(V.GS.dx), dy = wuni(V.GS.dy), g = wuni(V.GS.g), manning = wuni(V.GS.manning);
     const float rdx = wuni(V.GS.rdx), rdy = wuni(V.GS.rdy);
@@ -185,7 +188,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     // point sources inside this warp's window, in list order (the later one
     // wins on a shared cell, as the reference's assignment, cu:545)
     int nsrc = 0;
-    if (V.n_src > 0) {
+    if (GEN && V.n_src > 0) {
         const double area = V.dx * V.dy;
         for (int base = 0; base < V.n_src; base += 32) {
             const int s = base + lane;

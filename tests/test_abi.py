@@ -76,4 +76,8 @@ def test_describe_names_the_kernel_run(sw2d_mod):
     strip = int(d.split("strip_h=")[1].split()[0])
     units = int(d.split("units=")[1].split()[0])
     assert units == -(-200 // 27) * -(-300 // strip)  # column tiles x strips
+    # the forcing build follows the forcing: uniform rain, then the storm build
+    assert "forcing=uniform " in d
+    g.set_storm(50.0, 0.0, 0.0, 1.0, 0.0, 100.0)
+    assert "forcing=storm/sources " in g.describe()
     g.close()
