@@ -153,6 +153,46 @@ def test_stream_sources_storm_open_south(oracle_mod, sw2d_mod):
     assert bg["outflow"] == pytest.approx(bo["outflow"], rel=1e-3, abs=1e-3)
 
 
+def test_stream_forcing_forms_switch_mid_run(oracle_mod, sw2d_mod):
+    """The streaming kernel has a form for uniform rain and one carrying the
+    moving storm and the point sources; the launcher picks the form from the
+    handle's forcing whenever the launch graph is captured.  A run that goes
+    uniform rain -> storm with point sources -> uniform rain again (sources
+    cleared) follows the oracle through both forms and back."""
+    from sw2d import scenarios as S
+    O = oracle_mod
+    rows, cols = 64, 72
+    s = S.catchment(rows, dx=20.0, seed=17, cols=cols, manning=0.05)
+    o, g64 = make_pair(O, sw2d_mod, rows, cols, 20.0, s["z"], s["h0"], manning=0.05, south_open=1, dt_mode=1,
+                       dt=5.0)
+    g64.close()
+    g = _f32(sw2d_mod, rows, cols, 20.0, s["z"], s["h0"], manning=0.05, kernel=2, south_open=1, dt_mode=1, dt=5.0)
+    rain = np.array([40.0])
+    set_forcing(O, o, g, rain_kind=O.RAIN_STEP, rain=rain, rain_dt=3600.0)
+    assert "forcing=uniform " in g.describe()
+    o.advance(10 ** 6, t_end=200.0)
+    g.advance(10 ** 6, t_end=200.0)
+    storm = {"peak": 150.0, "x0": 0.0, "y0": 0.0, "vx": 1.5, "vy": 1.0, "sigma": 400.0}
+    cells = np.array([12 * cols + 30, 40 * cols + 5], dtype=np.int32)
+    q = np.array([[2.0, 1.0], [4.0, 0.5]])
+    set_forcing(O, o, g, storm=storm, sources=cells, src_q=q, dtoq=400.0)
+    assert "forcing=storm/sources " in g.describe()
+    o.advance(10 ** 6, t_end=400.0)
+    g.advance(10 ** 6, t_end=400.0)
+    g.set_point_sources(np.zeros(0, dtype=np.int32), np.zeros((1, 0)), 1.0)
+    set_forcing(O, o, g, rain_kind=O.RAIN_STEP, rain=rain, rain_dt=3600.0)
+    assert "forcing=uniform " in g.describe()
+    o.advance(10 ** 6, t_end=600.0)
+    g.advance(10 ** 6, t_end=600.0)
+    a, b = o.state()["h"], g.depth()
+    print("max |dh| =", max_abs(a, b))
+    assert max_abs(a, b) <= TOL_MM
+    bo, bg = o.budget(), g.budget()
+    assert bg["t"] == pytest.approx(600.0, abs=1e-9) and o.state()["t"] == pytest.approx(600.0, abs=1e-9)
+    assert bg["source_in"] == pytest.approx(bo["source_in"], rel=1e-4)
+    assert bg["rain_in"] == pytest.approx(bo["rain_in"], rel=1e-4)
+
+
 def test_f32_dam_break_front(oracle_mod, sw2d_mod):
     """A frictionless dam break is a moving discontinuity: at the same
     simulated time (the CFL step of each run follows its own thin-film tip
