@@ -9,16 +9,19 @@
 //     of one iteration (shortened by loading the neighbours' depths and
 //     discharges at the window's edges) -- and marches down a strip of rows
 //     (stream_unit in sw2d_stream_unit.cuh);
-//   * each row read from HBM (h, z, n, mask, um, vn; one coalesced line per
-//     field and warp) feeds a 3-row register pipeline
+//   * each row read from HBM (h, the face bed differences dzx and dzy, n,
+//     mask, um, vn and the depth remainder; one coalesced line per field and
+//     warp) feeds a 3-row register pipeline
 //         row r    : face depths and velocities uu1/vv1        (cu:363-453)
 //         row r-1  : new face discharges, momentum + dry bed   (cu:98-354)
 //         row r-2  : provisional depth, forcing at t           (cu:603-665)
 //         row r-3  : dry-cell fix per face (cu:695-725), final depth with
 //                    forcing at t+dt, CFL bound of the owned faces
 //     so every quantity is computed once per cell and row, in registers;
-//   * west/east neighbours come from warp shuffles; there is no shared-memory
-//     tile and no block-wide barrier inside the row loop;
+//   * west/east neighbours come from warp shuffles, except the neighbours'
+//     depths and discharges that each lane loads itself (they make the
+//     window's edge lanes exact); there is no shared-memory tile and no
+//     block-wide barrier inside the row loop;
 //   * the next row's loads are issued before the current row's arithmetic.
 //
 // Budgets and the CFL bound are reduced per warp and then per CTA; the last

@@ -230,9 +230,11 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         return storm_amp * __expf(-(x * x + y * y) / storm_2s2);
     };
 
-    // row loads: rows R0-4 .. R1+2 and columns gj0 .. gj0+31 all lie inside
-    // the zero frame around the domain, whose zeros are the inactive-cell and
-    // wall values, so no load needs a bounds test
+    // row loads: rows R0-4 .. R1+2 and columns gj0-1 .. gj0+32 (the window and
+    // the neighbours loaded at its edges; gj0 >= -3, and the last window ends
+    // 29 columns past the east wall) all lie inside the zero frame around the
+    // domain, whose zeros are the inactive-cell and wall values, so no load
+    // needs a bounds test
     float p_h, p_hw, p_hE, p_umE, p_vnE, p_dzx, p_dzy, p_n, p_um, p_vn, p_res;
     unsigned p_m;
     int gp = (R0 - 4) * pitch + gj;  // element offset of the next row to read (fields fit 32-bit offsets)
