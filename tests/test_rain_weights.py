@@ -100,6 +100,34 @@ def test_f32_rain_weights_within_bounds(oracle_mod, sw2d_mod):
 
 
 @pytest.mark.gpu
+def test_f32_rain_weights_times_storm_within_bounds(oracle_mod, sw2d_mod):
+    """The streaming kernel's form with both the rain factors and the moving
+    storm (and a point source) against the oracle."""
+    s, w = _scenario(rows=64, cols=90, seed=14)
+    O = oracle_mod
+    storm = {"peak": 200.0, "x0": 0.0, "y0": 0.0, "vx": 1.0, "vy": 0.5, "sigma": 300.0}
+    cells = np.array([30 * 90 + 45], dtype=np.int32)
+    q = np.array([[1.5], [0.5]])
+    o = O.Oracle(64, 90, 10.0, 10.0, s["z"], n=s["n"], dt_mode=1, dt=1.0, south_open=1)
+    o.set_state(s["h0"])
+    o.set_forcing(O.OracleForcing(rain_kind=O.RAIN_STORM, storm=storm, rain_w=w, sources=cells, src_q=q,
+                                  dtoq=300.0))
+    g = sw2d_mod.Solver(rows=64, cols=90, dx=10.0, dy=10.0, precision=sw2d_mod.PREC_F32, dt_mode=1, dt=1.0,
+                        south_open=1)
+    g.set_static(s["z"], s["n"])
+    g.set_state(s["h0"])
+    g.set_storm(storm["peak"], storm["x0"], storm["y0"], storm["vx"], storm["vy"], storm["sigma"])
+    g.set_point_sources(cells, q, 300.0)
+    g.set_rain_weights(w)
+    assert "forcing=storm/sources+rain_weights " in g.describe()
+    o.advance(10 ** 6, t_end=600.0)
+    g.advance(10 ** 6, t_end=600.0)
+    assert max_abs(o.state()["h"], g.depth()) <= 1e-3
+    assert g.budget()["rain_in"] == pytest.approx(o.budget()["rain_in"], rel=1e-4)
+    assert g.budget()["source_in"] == pytest.approx(o.budget()["source_in"], rel=1e-4)
+
+
+@pytest.mark.gpu
 def test_rain_weights_errors_and_reset(oracle_mod, sw2d_mod):
     s, w = _scenario()
     g = sw2d_mod.Solver(rows=36, cols=44, dx=10.0, dy=10.0)
