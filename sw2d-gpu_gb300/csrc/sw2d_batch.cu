@@ -166,7 +166,7 @@ int sw2d_batch_config_init(sw2d_batch_config *c) {
 }
 
 int sw2d_batch_scenario_bytes(const sw2d_config *cfg, int32_t n_rain, int32_t with_raster, int64_t *bytes) {
-    if (!cfg || !bytes || cfg->rows < 1 || cfg->cols < 1) return SW2D_ERR_INVALID_ARG;
+    if (!cfg || !bytes || !plane_fits_int32(cfg->rows, cfg->cols) || n_rain < 0) return SW2D_ERR_INVALID_ARG;
     *bytes = (int64_t)scenario_bytes(cfg, n_rain, with_raster != 0);
     return SW2D_OK;
 }

@@ -19,8 +19,11 @@ inline int pitch_for(int cols) { return ((cols + 34 + 31) / 32) * 32; }
 inline size_t plane_for(int rows, int pitch) { return (size_t)(kGhostTop + rows + 1 + kGhostBottom) * pitch; }
 inline size_t origin_for(int pitch) { return (size_t)kGhostTop * pitch + kGhostLeft; }
 // Kernels index a field, frame included, with 32-bit element offsets.
+// (rows and cols are bounded first, so that the int sums inside pitch_for and
+// plane_for cannot overflow)
 inline bool plane_fits_int32(int rows, int cols) {
-    return rows >= 1 && cols >= 1 && (long long)plane_for(rows, pitch_for(cols)) < (1ll << 31);
+    return rows >= 1 && cols >= 1 && rows < (1 << 30) && cols < (1 << 30) &&
+           (long long)plane_for(rows, pitch_for(cols)) < (1ll << 31);
 }
 
 // Core tiles supported by the step kernel instantiations.

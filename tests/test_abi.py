@@ -45,10 +45,24 @@ def test_invalid_configs_rejected_before_any_gpu_call(sw2d_mod):
     h = C.c_void_p()
     for kw in ({"rows": 0, "cols": 4}, {"rows": 4, "cols": 4, "dx": 0.0}, {"rows": 4, "cols": 4, "dt": -1.0},
                {"rows": 4, "cols": 4, "precision": 7}, {"rows": 4, "cols": 4, "dt_mode": 1, "cfl": 0.0},
-               {"rows": 60000, "cols": 60000}):  # beyond 32-bit field offsets
+               {"rows": 60000, "cols": 60000},  # beyond 32-bit field offsets
+               {"rows": 2 ** 31 - 1, "cols": 4}, {"rows": 4, "cols": 2 ** 31 - 1}):  # int sums would overflow
         c = sw2d_mod.default_config(**kw)
         assert L.sw2d_create(C.byref(c), C.byref(h)) == 1
     assert L.sw2d_create(None, C.byref(h)) == 1
+
+
+def test_batch_scenario_bytes_validates_its_arguments(sw2d_mod):
+    """The admission estimate needs no GPU and refuses what sw2d_batch_add
+    would refuse: a grid beyond 32-bit field offsets, a negative series."""
+    L = sw2d_mod.load()
+    n = C.c_int64()
+    ok = sw2d_mod.default_config(rows=64, cols=64, precision=sw2d_mod.PREC_F32, dt_mode=sw2d_mod.DT_CFL)
+    assert L.sw2d_batch_scenario_bytes(C.byref(ok), 3, 1, C.byref(n)) == 0 and n.value > 64 * 64 * 4
+    for kw in ({"rows": 60000, "cols": 60000}, {"rows": 4, "cols": 2 ** 31 - 1}, {"rows": 0, "cols": 4}):
+        c = sw2d_mod.default_config(**kw)
+        assert L.sw2d_batch_scenario_bytes(C.byref(c), 3, 1, C.byref(n)) == 1
+    assert L.sw2d_batch_scenario_bytes(C.byref(ok), -1, 1, C.byref(n)) == 1
 
 
 def test_device_bytes(sw2d_mod):
