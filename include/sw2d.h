@@ -190,8 +190,9 @@ int sw2d_get_field(sw2d_handle *h, int32_t field, double *out);
 /* Time, step count and FP64 mass budget of the current state. */
 int sw2d_get_budget(sw2d_handle *h, sw2d_budget *out);
 
-/* Depth at n cells (linear indices).  Replaces the WaterLevel.txt probe
- * loop cu:1386-1410. */
+/* Depth at n cells (linear indices i*cols + j; SW2D_ERR_INVALID_ARG if one
+ * lies outside the grid).  Replaces the WaterLevel.txt probe loop
+ * cu:1386-1410. */
 int sw2d_probe(sw2d_handle *h, const int32_t *cells, int32_t n, double *out);
 
 /* Checkpoint / restore (extension; the reference restarts only from a depth

@@ -763,6 +763,9 @@ int sw2d_probe(sw2d_handle *h, const int32_t *cells, int32_t n, double *out) {
     if (!h || (n > 0 && (!cells || !out))) return fail(h, SW2D_ERR_INVALID_ARG, "null argument");
     if (!h->have_state) return fail(h, SW2D_ERR_STATE, "no state");
     if (n <= 0) return SW2D_OK;
+    const long long ncell = (long long)h->cfg.rows * h->cfg.cols;
+    for (int s = 0; s < n; s++)
+        if (cells[s] < 0 || cells[s] >= ncell) return fail(h, SW2D_ERR_INVALID_ARG, "probe cell out of range");
     int rc = upload_table(h, h->probe_cells, cells, (size_t)n);
     if (rc) return rc;
     if (h->probe_out.bytes < (size_t)n * sizeof(double)) {

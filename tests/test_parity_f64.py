@@ -222,6 +222,10 @@ def test_probe_and_fields(oracle_mod, sw2d_mod):
     h = o.state()["h"]
     cells = np.array([0, 5, 16 * 32 - 1, 7 * 32 + 13], dtype=np.int32)
     assert np.array_equal(g.probe(cells), h.ravel()[cells])
+    for bad in (-1, 16 * 32):  # outside the grid: refused on the host
+        with pytest.raises(sw2d_mod.SW2DError) as e:
+            g.probe(np.array([3, bad], dtype=np.int32))
+        assert e.value.status == sw2d_mod.native.ERR_INVALID_ARG
     uu, vv = o.cell_velocity()
     assert same(g.field(sw2d_mod.FIELD_UU), uu)
     assert same(g.field(sw2d_mod.FIELD_VV), vv)
