@@ -27,6 +27,8 @@ from typing import Callable, Optional
 
 import numpy as np
 
+from .native import SW2DError
+
 
 @dataclasses.dataclass
 class Request:
@@ -52,6 +54,9 @@ class Server:
                  max_bytes: int, launches_per_tick: int = 24, keep_results: bool = False,
                  clock: Callable[[], float] = time.perf_counter, sleep: Callable[[float], None] = time.sleep):
         self.batch = batch_factory()
+        # scenario slots of the batch (0 = no limit known): a request waits for
+        # a free slot as it waits for memory
+        self.max_running = int(getattr(getattr(self.batch, "cfg", None), "max_scenarios", 0) or 0)
         self.bytes_of = bytes_of
         self.max_bytes = int(max_bytes)
         self.launches_per_tick = int(launches_per_tick)
@@ -84,9 +89,16 @@ class Server:
             waiting.append(heapq.heappop(self.pending))
         for item in waiting:
             req = item[2]
-            if self.bytes_used + req.bytes <= self.max_bytes:
-                sid = self.batch.add(req.cfg, req.z, req.depth, manning=req.manning, rain_kind=req.rain_kind,
-                                     rain=req.rain, rain_dt=req.rain_dt, t_end=req.t_end)
+            slot_free = not self.max_running or len(self.running) < self.max_running
+            if slot_free and self.bytes_used + req.bytes <= self.max_bytes:
+                try:
+                    sid = self.batch.add(req.cfg, req.z, req.depth, manning=req.manning, rain_kind=req.rain_kind,
+                                         rain=req.rain, rain_dt=req.rain_dt, t_end=req.t_end)
+                except (SW2DError, ValueError) as e:  # refused by the library: this request fails alone
+                    req.admitted = req.finished = self.now()
+                    req.result = {"error": str(e)}
+                    self.done.append(req)
+                    continue
                 req.admitted = self.now()
                 self.running[sid] = req
                 self.bytes_used += req.bytes
@@ -136,11 +148,15 @@ class Server:
     def stats(self):
         if not self.done:
             return {"requests": 0}
-        ttr = np.array([r.finished - r.arrival for r in self.done])
-        span = max(r.finished for r in self.done) - min(r.arrival for r in self.done)
-        cu = sum(int(r.cfg.rows) * int(r.cfg.cols) * int(r.result["steps"]) for r in self.done)
+        served = [r for r in self.done if "error" not in r.result]
+        if not served:
+            return {"requests": 0, "failed": len(self.done)}
+        ttr = np.array([r.finished - r.arrival for r in served])
+        span = max(r.finished for r in served) - min(r.arrival for r in served)
+        cu = sum(int(r.cfg.rows) * int(r.cfg.cols) * int(r.result["steps"]) for r in served)
         return {
-            "requests": len(self.done),
+            "requests": len(served),
+            "failed": len(self.done) - len(served),
             "p50_s": float(np.percentile(ttr, 50)),
             "p99_s": float(np.percentile(ttr, 99)),
             "mean_s": float(ttr.mean()),

@@ -113,3 +113,52 @@ def test_poisson_arrivals_rate():
     a = serve.poisson_arrivals(rate=10.0, n=5000, seed=1)
     assert np.all(np.diff(a) > 0)
     assert abs(len(a) / a[-1] - 10.0) < 0.5
+
+
+def test_admission_waits_for_a_free_scenario_slot():
+    """A batch with fewer scenario slots than the memory budget admits: the
+    extra requests wait for a slot instead of failing in batch.add."""
+    from sw2d import serve
+    clk = FakeClock()
+    fb = FakeBatch(clk)
+
+    class Slots:
+        max_scenarios = 2
+
+    fb.cfg = Slots()
+    real_add = fb.add
+
+    def add(*a, **k):
+        assert len(fb.scen) < 2, "the server overfilled the scenario table"
+        return real_add(*a, **k)
+
+    fb.add = add
+    srv = serve.Server(lambda: fb, bytes_of=lambda r: r._bytes, max_bytes=1000, launches_per_tick=10, clock=clk,
+                       sleep=clk.sleep)
+    st = srv.run([_req(serve, k, 0.0, 20, 10) for k in range(5)])
+    assert st["requests"] == 5 and st["failed"] == 0
+
+
+def test_a_refused_request_fails_alone():
+    """A request the library refuses (here: batch.add raises) finishes with
+    an error; the others are served."""
+    from sw2d import serve
+    from sw2d.native import SW2DError
+    clk = FakeClock()
+    fb = FakeBatch(clk)
+    real_add = fb.add
+
+    def add(cfg, z, depth, **k):
+        if k["t_end"] == 7.0:
+            raise SW2DError(1, "sw2d_batch_add")
+        return real_add(cfg, z, depth, **k)
+
+    fb.add = add
+    srv = serve.Server(lambda: fb, bytes_of=lambda r: r._bytes, max_bytes=100, launches_per_tick=10, clock=clk,
+                       sleep=clk.sleep)
+    reqs = [_req(serve, 0, 0.0, 20, 10), _req(serve, 1, 0.0, 7, 10), _req(serve, 2, 0.5, 20, 10)]
+    st = srv.run(reqs)
+    assert st["requests"] == 2 and st["failed"] == 1
+    bad = [r for r in srv.done if "error" in r.result]
+    assert [r.rid for r in bad] == [1] and "sw2d_batch_add" in bad[0].result["error"]
+    assert srv.bytes_used == 0 and not srv.running
