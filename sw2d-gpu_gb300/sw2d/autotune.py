@@ -28,7 +28,7 @@ RESIDENT_WARPS_PER_SM = (16, 20, 24)  # resident warps per SM of the kernel buil
 
 # Variant ids index the kernel builds of the library; a cache written for
 # another table of builds is not reused.
-TABLE_VERSION = "stream-v4"
+TABLE_VERSION = "stream-v5"
 
 
 def wave_strips(rows: int, cols: int, sms: int = 152, waves=(1, 2, 3, 4), warps_per_sm=RESIDENT_WARPS_PER_SM):
