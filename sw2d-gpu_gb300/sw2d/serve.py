@@ -78,6 +78,43 @@ class Server:
             raise ValueError(f"request {req.rid} needs {req.bytes} bytes, more than the budget {self.max_bytes}")
         heapq.heappush(self.pending, (req.arrival, req.rid, req))
 
+    def poll(self, rid):
+        """State of request `rid`: "pending", "running", "done", "failed",
+        "cancelled", or None if the server does not know it."""
+        for _, r, _req in self.pending:
+            if r == rid:
+                return "pending"
+        if any(req.rid == rid for req in self.running.values()):
+            return "running"
+        for req in self.done:
+            if req.rid == rid:
+                if req.result.get("cancelled"):
+                    return "cancelled"
+                return "failed" if "error" in req.result else "done"
+        return None
+
+    def cancel(self, rid) -> bool:
+        """Withdraws request `rid`: a pending one leaves the queue, a running
+        one is removed from the batch between ticks and its memory returned.
+        Returns False if the request is unknown or already finished."""
+        now = self.now() if self.t0 is not None else 0.0
+        for k, (_, r, req) in enumerate(self.pending):
+            if r == rid:
+                self.pending.pop(k)
+                heapq.heapify(self.pending)
+                req.finished, req.result = now, {"cancelled": True}
+                self.done.append(req)
+                return True
+        for sid, req in list(self.running.items()):
+            if req.rid == rid:
+                self.batch.remove(sid)
+                del self.running[sid]
+                self.bytes_used -= req.bytes
+                req.finished, req.result = now, {"cancelled": True}
+                self.done.append(req)
+                return True
+        return False
+
     # ---- one scheduling round ------------------------------------------------
     def now(self):
         return self.clock() - self.t0
@@ -148,15 +185,17 @@ class Server:
     def stats(self):
         if not self.done:
             return {"requests": 0}
-        served = [r for r in self.done if "error" not in r.result]
+        served = [r for r in self.done if "error" not in r.result and not r.result.get("cancelled")]
+        cancelled = sum(1 for r in self.done if r.result.get("cancelled"))
         if not served:
-            return {"requests": 0, "failed": len(self.done)}
+            return {"requests": 0, "failed": len(self.done) - cancelled, "cancelled": cancelled}
         ttr = np.array([r.finished - r.arrival for r in served])
         span = max(r.finished for r in served) - min(r.arrival for r in served)
         cu = sum(int(r.cfg.rows) * int(r.cfg.cols) * int(r.result["steps"]) for r in served)
         return {
             "requests": len(served),
-            "failed": len(self.done) - len(served),
+            "failed": len(self.done) - len(served) - cancelled,
+            "cancelled": cancelled,
             "p50_s": float(np.percentile(ttr, 50)),
             "p99_s": float(np.percentile(ttr, 99)),
             "mean_s": float(ttr.mean()),

@@ -162,3 +162,28 @@ def test_a_refused_request_fails_alone():
     bad = [r for r in srv.done if "error" in r.result]
     assert [r.rid for r in bad] == [1] and "sw2d_batch_add" in bad[0].result["error"]
     assert srv.bytes_used == 0 and not srv.running
+
+
+def test_poll_and_cancel():
+    """submit / poll / cancel: a pending request leaves the queue, a running
+    one leaves the batch and returns its memory; the rest are served."""
+    from sw2d import serve
+    clk = FakeClock()
+    fb = FakeBatch(clk)
+    srv = serve.Server(lambda: fb, bytes_of=lambda r: r._bytes, max_bytes=100, launches_per_tick=10, clock=clk,
+                       sleep=clk.sleep)
+    for r in (_req(serve, 0, 0.0, 50, 40), _req(serve, 1, 0.0, 50, 40), _req(serve, 2, 5.0, 50, 40)):
+        srv.submit(r)
+    srv.t0 = clk()
+    assert [srv.poll(k) for k in (0, 1, 2, 9)] == ["pending", "pending", "pending", None]
+    srv.step()  # admits 0 and 1 (80 of 100 bytes); 2 arrives later
+    assert srv.poll(0) == "running" and srv.poll(2) == "pending" and srv.bytes_used == 80
+    assert srv.cancel(1) and srv.poll(1) == "cancelled" and srv.bytes_used == 40
+    assert [sid for sid, _ in fb.removes] == [1]
+    assert srv.cancel(2) and srv.poll(2) == "cancelled" and not srv.pending
+    assert not srv.cancel(1) and not srv.cancel(9)
+    while srv.pending or srv.running:
+        srv.step()
+    st = srv.stats()
+    assert srv.poll(0) == "done"
+    assert st["requests"] == 1 and st["cancelled"] == 2 and st["failed"] == 0
