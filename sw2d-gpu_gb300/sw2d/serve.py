@@ -159,6 +159,8 @@ class Server:
 
     def step(self):
         """Admit, advance one tick if anything is resident, retire."""
+        if self.t0 is None:  # the server's clock starts at its first step
+            self.t0 = self.clock()
         self._admit()
         if self.running:
             self.batch.advance(self.launches_per_tick, wait=False)
@@ -171,7 +173,8 @@ class Server:
         """Serves `requests` (plus anything submitted before) until all are done."""
         for r in requests:
             self.submit(r)
-        self.t0 = self.clock()
+        if self.t0 is None:
+            self.t0 = self.clock()
         while self.pending or self.running:
             if timeout is not None and self.now() > timeout:
                 raise TimeoutError(f"{len(self.pending)} pending and {len(self.running)} running after {timeout} s")

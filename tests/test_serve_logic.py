@@ -174,9 +174,8 @@ def test_poll_and_cancel():
                        sleep=clk.sleep)
     for r in (_req(serve, 0, 0.0, 50, 40), _req(serve, 1, 0.0, 50, 40), _req(serve, 2, 5.0, 50, 40)):
         srv.submit(r)
-    srv.t0 = clk()
     assert [srv.poll(k) for k in (0, 1, 2, 9)] == ["pending", "pending", "pending", None]
-    srv.step()  # admits 0 and 1 (80 of 100 bytes); 2 arrives later
+    srv.step()  # starts the clock, admits 0 and 1 (80 of 100 bytes); 2 arrives later
     assert srv.poll(0) == "running" and srv.poll(2) == "pending" and srv.bytes_used == 80
     assert srv.cancel(1) and srv.poll(1) == "cancelled" and srv.bytes_used == 40
     assert [sid for sid, _ in fb.removes] == [1]
