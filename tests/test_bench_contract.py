@@ -1,0 +1,46 @@
+"""bench.py's reference arm on the host cores: the JSON line's contract (keys,
+units, steps, the zero-copy e2e of a CPU run) and the rank rule under
+torchrun (rank 0 alone prints)."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _run(extra_env=None, args=("--steps", "3", "--warmup", "3")):
+    env = dict(os.environ)
+    env.update(extra_env or {})
+    return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", *args],
+                          cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+
+
+def test_reference_arm_json_line():
+    p = _run()
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == "cell-updates/s" and d["unit"] == "cell-updates/s"
+    assert d["value"] > 0 and d["higher_is_better"] is True
+    assert d["steps"] == 3 and d["warmup"] == 3 and d["n_gpus"] == 1
+    cb = d["cpu_baseline"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+    assert d["config"]["grid"] == [2048, 2048]
+
+
+def test_reference_arm_warmup_floor():
+    """Fewer than 3 warm-up steps are raised to 3."""
+    p = _run(args=("--steps", "1", "--warmup", "0"))
+    assert p.returncode == 0, p.stderr[-2000:]
+    d = json.loads([ln for ln in p.stdout.splitlines() if ln.startswith("{")][0])
+    assert d["warmup"] == 3 and d["steps"] == 1
+
+
+def test_reference_arm_other_ranks_print_nothing():
+    p = _run({"RANK": "1", "LOCAL_RANK": "1", "WORLD_SIZE": "2"})
+    assert p.returncode == 0, p.stderr[-2000:]
+    assert not [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
