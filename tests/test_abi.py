@@ -95,3 +95,43 @@ def test_describe_names_the_kernel_run(sw2d_mod):
     g.set_storm(50.0, 0.0, 0.0, 1.0, 0.0, 100.0)
     assert "forcing=storm/sources " in g.describe()
     g.close()
+
+
+C_CALLER = r"""
+#include <math.h>
+#include <stdio.h>
+#include "sw2d.h"
+
+int main(void) {
+    sw2d_config cfg;
+    if (sw2d_config_init(&cfg) != SW2D_OK) return 1;
+    if (cfg.g != 9.80 || cfg.th != 1.0e-4 || cfg.precision != SW2D_PREC_F64) return 2;
+    cfg.rows = 0; /* invalid: refused before any device call */
+    sw2d_handle *h = NULL;
+    if (sw2d_create(&cfg, &h) != SW2D_ERR_INVALID_ARG || h != NULL) return 3;
+    int64_t n = 0;
+    cfg.rows = cfg.cols = 64;
+    cfg.dx = cfg.dy = 1.0;
+    if (sw2d_device_bytes(&cfg, &n) != SW2D_OK || n <= 0) return 4;
+    printf("%s|%s|%lld\n", sw2d_status_string(SW2D_OK), sw2d_status_string(SW2D_ERR_NONFINITE), (long long)n);
+    return 0;
+}
+"""
+
+
+def test_header_compiles_as_c99_and_links(sw2d_mod, tmp_path):
+    """A plain C99 caller (no C++ anywhere) includes the header, links the
+    library and calls it: the extern "C" boundary as a C driver sees it."""
+    from sw2d import native
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    lib_dir = os.path.dirname(native.LIB_PATH)
+    cc = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I",
+                         os.path.join(ROOT, "include"), str(src), "-o", str(exe), "-L", lib_dir, "-lsw2d",
+                         f"-Wl,-rpath,{lib_dir}", "-lm"], capture_output=True, text=True)
+    assert cc.returncode == 0, cc.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0, (run.returncode, run.stderr)
+    ok, nonfinite, nbytes = run.stdout.strip().split("|")
+    assert ok == "ok" and "non-finite" in nonfinite and int(nbytes) > 64 * 64 * 8
