@@ -70,3 +70,46 @@ def test_nan_depth_gives_nan_faces_in_the_oracle(oracle_mod):
     o.advance(1, 1e9)
     st = o.state()
     assert np.isnan(st["um"]).any() or np.isnan(st["vn"]).any()
+
+
+def test_lake_at_rest_stays_at_rest(oracle_mod):
+    """A flat water surface over an uneven bed, every cell wet, with Manning
+    friction: the surface-slope term vanishes and no dry-bed rule applies.
+    On a bed of dyadic elevations (every sum exact) the state does not move
+    at all.  On an arbitrary bed it moves only by FP64 rounding: the
+    reference evaluates the slope as ((hb + zb) - ha) - za (cu:166), which
+    rounds even when hb + zb == ha + za exactly."""
+    O = oracle_mod
+    rows, cols = 40, 56
+    z = np.random.default_rng(3).uniform(0.0, 2.0, (rows, cols))
+    for bed, tol in ((np.round(z * 64.0) / 64.0, 0.0), (z, 1e-12)):
+        h0 = 3.0 - bed
+        o = O.Oracle(rows, cols, 5.0, 5.0, bed, manning=0.03, dt_mode=0, dt=0.1)
+        o.set_state(h0)
+        o.advance(200, 1e9)
+        st = o.state()
+        assert np.max(np.abs(st["h"] - h0)) <= tol
+        assert np.max(np.abs(st["um"])) <= 10 * tol and np.max(np.abs(st["vn"])) <= 10 * tol
+
+
+def test_budget_closes_with_open_edge_rain_sources_evaporation(oracle_mod):
+    """Stored volume = initial + rain + sources - evaporation - outflow through
+    the open south edge + water created by the depth clamp, to FP64 rounding,
+    on a run that uses every forcing at once."""
+    from sw2d import scenarios as S
+    O = oracle_mod
+    rows, cols = 48, 40
+    s = S.catchment(rows, dx=10.0, seed=6, cols=cols)
+    o = O.Oracle(rows, cols, 10.0, 10.0, s["z"], n=s["n"], dt_mode=1, dt=1.0, cfl=0.5, south_open=1,
+                 EV_WL_min=0.001, INT=0.1, INF=0.2, LWL=0.05)
+    o.set_state(s["h0"])
+    v0 = o.volume()
+    cells = np.array([5 * cols + 7, 30 * cols + 20], dtype=np.int32)
+    q = np.array([[1.0, 0.5], [2.0, 0.0], [0.5, 1.5]])
+    o.set_forcing(O.OracleForcing(rain_kind=O.RAIN_LINEAR, rain=np.array([30.0, 90.0, 10.0]), rain_dt=300.0,
+                                  ev=np.array([5e-7, 8e-7]), ev_dt=600.0, sources=cells, src_q=q, dtoq=300.0))
+    o.advance(10 ** 6, t_end=900.0)
+    b = o.budget()
+    assert b["rain_in"] > 0 and b["source_in"] > 0 and b["evap_out"] > 0 and b["outflow"] > 0
+    expect = v0 + b["rain_in"] + b["source_in"] - b["evap_out"] - b["outflow"] + b["clamp_gain"]
+    assert abs(o.volume() - expect) <= 1e-9 * max(v0, 1.0)
