@@ -113,3 +113,27 @@ def test_budget_closes_with_open_edge_rain_sources_evaporation(oracle_mod):
     assert b["rain_in"] > 0 and b["source_in"] > 0 and b["evap_out"] > 0 and b["outflow"] > 0
     expect = v0 + b["rain_in"] + b["source_in"] - b["evap_out"] - b["outflow"] + b["clamp_gain"]
     assert abs(o.volume() - expect) <= 1e-9 * max(v0, 1.0)
+
+
+def test_transposed_problem_gives_the_transposed_solution(oracle_mod):
+    """The x-face (cu:116-225) and y-face (cu:232-342) updates are mirror
+    images, including the column-0 / row-0 rules, so solving the transposed
+    problem (rows <-> cols, dx <-> dy, um <-> vn) gives the transposed
+    solution, bit for bit, here with dx != dy, per-cell n and rain.  An
+    index slip in either direction breaks this."""
+    from sw2d import scenarios as S
+    O = oracle_mod
+    s = S.catchment(36, dx=10.0, seed=4, cols=52)
+
+    def run(z, n, h0, dx, dy):
+        o = O.Oracle(z.shape[0], z.shape[1], dx, dy, z, n=n, dt_mode=0, dt=0.5)
+        o.set_state(h0)
+        o.set_forcing(O.OracleForcing(rain_kind=O.RAIN_STEP, rain=np.array([60.0]), rain_dt=3600.0))
+        o.advance(400, 1e9)
+        return o.state()
+
+    a = run(s["z"], s["n"], s["h0"], 10.0, 8.0)
+    b = run(s["z"].T.copy(), s["n"].T.copy(), s["h0"].T.copy(), 8.0, 10.0)
+    assert np.array_equal(a["h"], b["h"].T)
+    assert np.array_equal(a["um"], b["vn"].T) and np.array_equal(a["vn"], b["um"].T)
+    assert a["h"].max() > s["h0"].max()  # the rain did something
