@@ -181,6 +181,7 @@ class Solver:
             raise SW2DError(st, f"{what}: {msg}")
 
     def close(self):
+        """Frees the handle and its device memory (sw2d_destroy); safe to call twice."""
         if getattr(self, "_h", None):
             load().sw2d_destroy(self._h)
             self._h = None
@@ -199,12 +200,16 @@ class Solver:
 
     # -- inputs ---------------------------------------------------------
     def set_static(self, z, manning=None):
+        """DEM z and an optional per-cell Manning raster, (rows, cols) float64, north row first; cells at
+        cfg.nodata are inactive."""
         r, c = self.rows, self.cols
         z = _f64(z, (r, c))
         n = _f64(manning, (r, c)) if manning is not None else None
         self._check(load().sw2d_set_static(self._h, _p(z), _p(n)), "sw2d_set_static")
 
     def set_state(self, depth, um=None, vn=None, t0=0.0):
+        """Depth (rows, cols) and optional discharges um (rows+1, cols) and vn (rows, cols+1) at time t0; resets
+        the budgets."""
         r, c = self.rows, self.cols
         d = _f64(depth, (r, c))
         u = _f64(um, (r + 1, c)) if um is not None else None
@@ -212,11 +217,15 @@ class Solver:
         self._check(load().sw2d_set_state(self._h, _p(d), _p(u), _p(v), float(t0)), "sw2d_set_state")
 
     def set_rain(self, kind, series=None, dt_series=1.0):
+        """Uniform rain: a RAIN_* kind and its series (COMPAT: the reference's formula; STEP, LINEAR: mm/h) every
+        dt_series seconds."""
         s = _f64(np.atleast_1d(series)) if series is not None else None
         n = 0 if s is None else s.size
         self._check(load().sw2d_set_rain(self._h, int(kind), _p(s), n, float(dt_series)), "sw2d_set_rain")
 
     def set_storm(self, peak, x0, y0, vx, vy, sigma, t_stop=1e300):
+        """Moving Gaussian storm cell: peak [mm/h], centre (x0 + vx t, y0 + vy t) [m], width sigma [m], until
+        t_stop [s]."""
         self._check(load().sw2d_set_storm(self._h, peak, x0, y0, vx, vy, sigma, t_stop), "sw2d_set_storm")
 
     def set_rain_weights(self, w=None):
@@ -228,11 +237,14 @@ class Solver:
         self._check(load().sw2d_set_rain_weights(self._h, _p(w)), "sw2d_set_rain_weights")
 
     def set_evaporation(self, series=None, dt_series=1.0):
+        """Evaporation series [m/s] every dt_series seconds, applied where the depth exceeds cfg.EV_WL_min."""
         s = _f64(np.atleast_1d(series)) if series is not None else None
         n = 0 if s is None else s.size
         self._check(load().sw2d_set_evaporation(self._h, _p(s), n, float(dt_series)), "sw2d_set_evaporation")
 
     def set_point_sources(self, cells, q, dtoq):
+        """Point sources at linear cell indices with a (records, sources) table of rates [m^3/s] every dtoq
+        seconds; an empty cells array removes them."""
         cells = np.ascontiguousarray(cells, dtype=np.int32)
         q = _f64(np.asarray(q).reshape(-1, max(cells.size, 1)))
         self._check(load().sw2d_set_point_sources(self._h, _p(cells), cells.size, _p(q), q.shape[0], float(dtoq)),
@@ -240,19 +252,23 @@ class Solver:
 
     # -- running --------------------------------------------------------
     def advance(self, max_steps, t_end=1e300):
+        """Advances up to max_steps iterations, stopping at t_end; returns the iterations done."""
         done = C.c_int64()
         self._check(load().sw2d_advance(self._h, int(max_steps), float(t_end), C.byref(done)), "sw2d_advance")
         return int(done.value)
 
     def synchronize(self):
+        """Waits for the work queued on the handle's stream."""
         self._check(load().sw2d_synchronize(self._h), "sw2d_synchronize")
 
     def stream(self) -> int:
+        """The handle's CUDA stream (a cudaStream_t as an int)."""
         s = C.c_void_p()
         self._check(load().sw2d_get_stream(self._h, C.byref(s)), "sw2d_get_stream")
         return int(s.value or 0)
 
     def launch_count(self) -> int:
+        """Step-kernel launches issued so far."""
         n = C.c_int64()
         self._check(load().sw2d_launch_count(self._h, C.byref(n)), "sw2d_launch_count")
         return int(n.value)
@@ -265,6 +281,7 @@ class Solver:
 
     # -- outputs --------------------------------------------------------
     def field(self, which):
+        """One FIELD_* raster as float64: (rows, cols), (rows+1, cols) for FIELD_UM, (rows, cols+1) for FIELD_VN."""
         r, c = self.rows, self.cols
         shape = {FIELD_UM: (r + 1, c), FIELD_VN: (r, c + 1)}.get(which, (r, c))
         out = np.empty(shape, dtype=np.float64)
@@ -272,12 +289,16 @@ class Solver:
         return out
 
     def depth(self):
+        """The depth raster (rows, cols)."""
         return self.field(FIELD_DEPTH)
 
     def state(self):
+        """h, um and vn as float64 arrays in a dict."""
         return {"h": self.field(FIELD_DEPTH), "um": self.field(FIELD_UM), "vn": self.field(FIELD_VN)}
 
     def budget(self):
+        """Time, iterations and the FP64 budgets (volume, rain, sources, evaporation, outflow, clamp gain) as a
+        dict."""
         b = Budget()
         self._check(load().sw2d_get_budget(self._h, C.byref(b)), "sw2d_get_budget")
         return {k: getattr(b, k) for k, _ in Budget._fields_ if k != "reserved"}
@@ -291,9 +312,11 @@ class Solver:
         return buf.raw
 
     def restore(self, ckpt: bytes):
+        """Loads a checkpoint() taken from a handle of the same configuration; the run continues bit for bit."""
         self._check(load().sw2d_checkpoint_load(self._h, ckpt, len(ckpt)), "sw2d_checkpoint_load")
 
     def probe(self, cells):
+        """Depth at linear cell indices i*cols + j; an index outside the grid raises SW2DError."""
         cells = np.ascontiguousarray(cells, dtype=np.int32)
         out = np.empty(cells.size, dtype=np.float64)
         self._check(load().sw2d_probe(self._h, _p(cells), cells.size, _p(out)), "sw2d_probe")
@@ -336,6 +359,7 @@ class Batch:
             raise SW2DError(st, f"{what}: {load().sw2d_batch_last_error(self._h).decode()}")
 
     def close(self):
+        """Frees the batch, its scenarios and their device memory; safe to call twice."""
         if getattr(self, "_h", None):
             load().sw2d_batch_destroy(self._h)
             self._h = None
@@ -353,6 +377,8 @@ class Batch:
         self.close()
 
     def add(self, cfg: Config, z, depth, manning=None, rain_kind=RAIN_NONE, rain=None, rain_dt=1.0, t_end=1e300):
+        """Admits one FP32 CFL scenario (rasters as for Solver, a series rain kind) running to t_end; returns its
+        id."""
         r, c = cfg.rows, cfg.cols
         z = _f64(z, (r, c))
         d = _f64(depth, (r, c))
@@ -366,12 +392,14 @@ class Batch:
         return sid.value
 
     def advance(self, launches, wait=True):
+        """Issues `launches` iterations for every running scenario; with wait, returns how many still run."""
         run = C.c_int32()
         self._check(load().sw2d_batch_advance(self._h, int(launches), C.byref(run) if wait else None),
                     "sw2d_batch_advance")
         return run.value if wait else None
 
     def poll(self):
+        """{id: {running, t, steps}} for every resident scenario."""
         cap = max(len(self.shapes), 1)
         ids = np.zeros(cap, np.int32); run = np.zeros(cap, np.int32); t = np.zeros(cap); steps = np.zeros(cap, np.int64)
         n = C.c_int32()
@@ -382,6 +410,7 @@ class Batch:
                 for i, rr, tt, ss in zip(ids[:k], run[:k], t[:k], steps[:k])}
 
     def field(self, sid, which=FIELD_DEPTH):
+        """One FIELD_* raster of scenario sid, shaped as Solver.field."""
         r, c = self.shapes[sid]
         shape = {FIELD_UM: (r + 1, c), FIELD_VN: (r, c + 1)}.get(which, (r, c))
         out = np.empty(shape)
@@ -389,25 +418,30 @@ class Batch:
         return out
 
     def budget(self, sid):
+        """The FP64 budgets of scenario sid, as Solver.budget."""
         b = Budget()
         self._check(load().sw2d_batch_get_budget(self._h, int(sid), C.byref(b)), "sw2d_batch_get_budget")
         return {k: getattr(b, k) for k, _ in Budget._fields_ if k != "reserved"}
 
     def remove(self, sid):
+        """Removes scenario sid and frees its memory in stream order."""
         self._check(load().sw2d_batch_remove(self._h, int(sid)), "sw2d_batch_remove")
         self.shapes.pop(sid, None)
 
     def bytes_in_use(self):
+        """Device bytes held by the resident scenarios."""
         v = C.c_int64()
         self._check(load().sw2d_batch_bytes_in_use(self._h, C.byref(v)), "sw2d_batch_bytes_in_use")
         return int(v.value)
 
     def stream(self):
+        """The batch's CUDA stream (a cudaStream_t as an int)."""
         s = C.c_void_p()
         self._check(load().sw2d_batch_get_stream(self._h, C.byref(s)), "sw2d_batch_get_stream")
         return int(s.value or 0)
 
     def launch_count(self):
+        """Batch-kernel launches issued so far."""
         v = C.c_int64()
         self._check(load().sw2d_batch_launch_count(self._h, C.byref(v)), "sw2d_batch_launch_count")
         return int(v.value)
