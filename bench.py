@@ -250,8 +250,13 @@ def run_ours(args):
     ge.close()
     del h_pinned
     e2e_value = active * CHUNK * k_e2e / te
-    h2d = (SIZE * SIZE * 8) * 2 + (SIZE * SIZE * 8) + ((SIZE + 1) * SIZE * 8) * 2  # z, n, h, um, vn
-    d2h = SIZE * SIZE * 8 + k_e2e * (1024 * 8 + 200)
+    # bytes the library copies (sw2d_api.cu): set_static z, n; set_state h, um, vn and the
+    # initial clock slot, then one clock read and one budget read (1024 volume partials);
+    # the rain table; per advance one Control down and one clock slot up; per budget the
+    # volume partials; the final depth
+    clock_b, control_b, partials_b = 1120, 16, 1024 * 8
+    h2d = (SIZE * SIZE * 8) * 3 + ((SIZE + 1) * SIZE * 8) * 2 + clock_b + 8 + k_e2e * control_b
+    d2h = (clock_b + partials_b) + k_e2e * (clock_b + partials_b) + SIZE * SIZE * 8
     assert np.isfinite(out_h).all()
 
     # ---- batched ensemble and served stream (extra keys) --------------------

@@ -44,3 +44,29 @@ def test_reference_arm_other_ranks_print_nothing():
     p = _run({"RANK": "1", "LOCAL_RANK": "1", "WORLD_SIZE": "2"})
     assert p.returncode == 0, p.stderr[-2000:]
     assert not [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
+
+
+def test_e2e_byte_counts_match_the_library_structs(tmp_path):
+    """bench.py counts the e2e leg's copies with the sizes of the clock slot,
+    the control block and the volume partials; they must be the library's."""
+    import re
+    import shutil
+    import pytest
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not found")
+    src = tmp_path / "sizes.cu"
+    src.write_text('#include "sw2d_launch.h"\n#include <cstdio>\n'
+                   'int main() { std::printf("%zu %zu %zu\\n", sizeof(sw2d::Clock), sizeof(sw2d::Control), '
+                   '(size_t)sw2d::kVolumeBlocks * sizeof(double)); return 0; }\n')
+    exe = tmp_path / "sizes"
+    csrc = os.path.join(ROOT, "sw2d-gpu_gb300", "csrc")
+    cc = subprocess.run([nvcc, "-std=c++17", "-I", os.path.join(ROOT, "include"), "-I", csrc, str(src), "-o",
+                         str(exe)], capture_output=True, text=True)
+    assert cc.returncode == 0, cc.stderr[-2000:]
+    clock_b, control_b, partials_b = map(int, subprocess.run([str(exe)], capture_output=True, text=True,
+                                                              check=True).stdout.split())
+    bench = open(os.path.join(ROOT, "bench.py")).read()
+    m = re.search(r"clock_b, control_b, partials_b = (\d+), (\d+), (\d+) \* 8", bench)
+    assert m, "bench.py's byte constants not found"
+    assert (int(m.group(1)), int(m.group(2)), int(m.group(3)) * 8) == (clock_b, control_b, partials_b)
