@@ -41,3 +41,20 @@ def test_tune_small_grid_on_gpu(sw2d_mod, tmp_path):
     assert cfg.strip_h == best["strip_h"] and cfg.variant == best["variant"]
     g = sw2d_mod.Solver(cfg)  # the tuned configuration runs
     g.close()
+
+
+def test_wave_strips_include_the_library_choice():
+    """The autotuner's wave-fitting strips use the kernel's window width
+    (27 output columns) and contain the strip the library picks itself:
+    at 2048^2 on 152 SMs with the default 20-warp build, 76 column tiles x
+    40 strips of 52 rows fill exactly one wave of 3040 warps (the
+    decomposition sw2d_describe reports on GB300)."""
+    from sw2d import autotune
+    assert autotune.OUT_COLS == 27
+    strips = autotune.wave_strips(2048, 2048, sms=152, waves=(1,), warps_per_sm=(20,))
+    assert strips == [52]
+    tiles = -(-2048 // autotune.OUT_COLS)
+    assert tiles * -(-2048 // 52) == 152 * 20
+    # more waves give shorter strips, never below 16 rows
+    many = autotune.wave_strips(2048, 2048, sms=152)
+    assert min(many) >= 16 and 52 in many and max(many) >= 52
