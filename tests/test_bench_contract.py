@@ -70,3 +70,22 @@ def test_e2e_byte_counts_match_the_library_structs(tmp_path):
     m = re.search(r"clock_b, control_b, partials_b = (\d+), (\d+), (\d+) \* 8", bench)
     assert m, "bench.py's byte constants not found"
     assert (int(m.group(1)), int(m.group(2)), int(m.group(3)) * 8) == (clock_b, control_b, partials_b)
+
+
+def test_depth_error_known_answers():
+    """The accuracy figures bench.py reports (max |dh|, its 99.99th
+    percentile, the flooded-area difference) on a constructed case."""
+    import importlib.util
+    import numpy as np
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    a = np.zeros((200, 50))
+    a[:100] = 0.3                  # 5000 wet cells
+    b = a.copy()
+    b[5, :4] += 7e-4               # 4 cells differ by 0.7 mm
+    b[150, 0] = 2e-4               # one cell wet in b only
+    e = bench.depth_error(a, b)
+    assert abs(e["max_abs_dh_m"] - 7e-4) < 1e-15
+    assert e["flooded_area_rel_diff"] == 1 / 5000
+    assert 0.0 <= e["p9999_abs_dh_m"] <= e["max_abs_dh_m"]
