@@ -135,3 +135,16 @@ def test_header_compiles_as_c99_and_links(sw2d_mod, tmp_path):
     assert run.returncode == 0, (run.returncode, run.stderr)
     ok, nonfinite, nbytes = run.stdout.strip().split("|")
     assert ok == "ok" and "non-finite" in nonfinite and int(nbytes) > 64 * 64 * 8
+
+
+def test_invalid_batch_configs_rejected_before_any_gpu_call(sw2d_mod):
+    from sw2d import native
+    L = sw2d_mod.load()
+    h = C.c_void_p()
+    for kw in ({"chunk": 4}, {"chunk": 0}, {"max_scenarios": 0}, {"max_units": 0}, {"strip_h": -1}):
+        c = native.batch_config(**kw)
+        assert L.sw2d_batch_create(C.byref(c), C.byref(h)) == 1, kw
+        assert not h.value
+    assert L.sw2d_batch_create(None, C.byref(h)) == 1
+    with pytest.raises(AttributeError):
+        native.batch_config(no_such_field=1)
