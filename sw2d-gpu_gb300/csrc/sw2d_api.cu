@@ -646,7 +646,7 @@ int sw2d_advance(sw2d_handle *h, int64_t max_steps, double t_end, int64_t *steps
     *h->h_ctl = ctl;
     CK(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Control), cudaMemcpyHostToDevice, h->stream));
     // plan the next launch under the new control and the current forcing
-    plan_kernel<<<1, 1, 0, h->stream>>>(h->G, h->F, h->d_clk, h->d_ctl, (int)(h->launches % 3));
+    plan_kernel<<<1, 32, 0, h->stream>>>(h->G, h->F, h->d_clk, h->d_ctl, (int)(h->launches % 3));
     CK(h, cudaGetLastError());
     for (;;) {
         double dtn;

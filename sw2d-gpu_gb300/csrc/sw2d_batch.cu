@@ -403,7 +403,7 @@ int sw2d_batch_add(sw2d_batch *b, const sw2d_config *cfg, const double *z, const
     BCK(b, cudaMemcpyAsync(clk + cur, b->h_clk, sizeof(Clock), cudaMemcpyHostToDevice, b->stream));
     BCK(b, launch_cmax(d.h[0], d.um[0], d.vn[0], m_dev, cfg->rows, cfg->cols, h.pitch, G.south_open, d.T.ge_th,
                        cfg->g, &clk[cur].cmax_bits, b->stream));
-    plan_kernel<<<1, 1, 0, b->stream>>>(G, F, clk, &b->d_scen[slot].ctl, cur);
+    plan_kernel<<<1, 32, 0, b->stream>>>(G, F, clk, &b->d_scen[slot].ctl, cur);
     BCK(b, cudaGetLastError());
     ScenarioStatus s0;
     std::memset(&s0, 0, sizeof(s0));

@@ -135,15 +135,18 @@ __global__ void __launch_bounds__(NWARP * 32, MINB) batch_step_kernel(const Batc
                 if (A.too_many_sources) atomicOr(&S.clk[slot_out].status, (unsigned)ST_TOO_MANY_LOCAL_SOURCES);
             }
         }
+        unsigned ticket = 0u;
         if (lane == 0) {
             __threadfence();
-            const unsigned ticket = atomicAdd(&S.clk[slot_out].done_blocks, 1u);
-            if (ticket == (unsigned)S.nunits - 1u) {
-                __threadfence();
-                if (run) finalize_slot(ci, S.clk[slot_out], S.clk[slot_nx], ci.plan, S.ctl, S.G, S.F);
-                else carry_slot(ci, S.clk[slot_out], S.clk[slot_nx]);
-                write_status(S.clk[slot_out], S.status);
-            }
+            ticket = atomicAdd(&S.clk[slot_out].done_blocks, 1u);
+        }
+        ticket = __shfl_sync(0xffffffffu, ticket, 0);
+        if (ticket == (unsigned)S.nunits - 1u) {  // the scenario's last unit: the whole warp finalises
+            __threadfence();
+            if (run) finalize_slot_warp(lane, ci, S.clk[slot_out], S.clk[slot_nx], ci.plan, S.ctl, S.G, S.F);
+            else if (lane == 0) carry_slot(ci, S.clk[slot_out], S.clk[slot_nx]);
+            __syncwarp();
+            if (lane == 0) write_status(S.clk[slot_out], S.status);
         }
         __syncwarp();
     }

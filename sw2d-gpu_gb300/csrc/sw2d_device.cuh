@@ -238,9 +238,16 @@ __device__ inline double source_rate(const ForcingDesc &F, int n_src, int s, dou
     return q / area;
 }
 
-// The plan of the launch that reads clock slot c under control ctl.
-__device__ inline Plan make_plan(double t, unsigned long long cmax_bits, long long steps, const Control &ctl,
-                                 const GridDesc &G, const ForcingDesc &F) {
+// The plan of the launch that reads clock slot c under control ctl.  Called
+// by all 32 lanes of one converged warp; every lane returns the same plan.
+// FP64 arithmetic on this GPU has long latencies (a division takes several
+// hundred cycles) and the plan lies on the critical path between two
+// launches, so the pairs of independent evaluations -- the forcing at t0 and
+// at t1, dt2/dx and dt2/dy -- run as one instruction stream on lanes 0 and 1
+// instead of one after the other.  Each value is computed by the same
+// operations as a serial evaluation would use.
+__device__ inline Plan make_plan_warp(const int lane, double t, unsigned long long cmax_bits, long long steps,
+                                      const Control &ctl, const GridDesc &G, const ForcingDesc &F) {
     Plan p;
     p.run = 0;
     p.storm_on0 = p.storm_on1 = 0;
@@ -253,24 +260,31 @@ __device__ inline Plan make_plan(double t, unsigned long long cmax_bits, long lo
     d.rr0 = d.rr1 = d.ev0 = d.ev1 = 0.0;
     d.sx0 = d.sy0 = d.sx1 = d.sy1 = 0.0;
     double dt = 0.0;
-    if (decide_step(t, __longlong_as_double((long long)cmax_bits), steps, ctl, G, &dt)) {
+    if (decide_step(t, __longlong_as_double((long long)cmax_bits), steps, ctl, G, &dt)) {  // warp-uniform
         p.run = 1;
         p.dt = dt;
         p.t1 = t + dt;
         d.dt2 = 2.00 * dt;
-        d.dt2dx = d.dt2 / G.dx;
-        d.dt2dy = d.dt2 / G.dy;
-        d.rr0 = rain_uniform(F, p.t0);
-        d.rr1 = rain_uniform(F, p.t1);
-        d.ev0 = evap_rate(F, p.t0);
-        d.ev1 = evap_rate(F, p.t1);
+        const bool second = (lane & 1) != 0;  // lane 1: t1 and the y step; lane 0: t0 and the x step
+        const double tl = second ? p.t1 : p.t0;
+        const double q = d.dt2 / (second ? G.dy : G.dx);
+        const double rr = rain_uniform(F, tl);
+        const double ev = evap_rate(F, tl);
+        const double sx = F.storm_x0 + F.storm_vx * tl;
+        const double sy = F.storm_y0 + F.storm_vy * tl;
+        d.dt2dx = __shfl_sync(0xffffffffu, q, 0);
+        d.dt2dy = __shfl_sync(0xffffffffu, q, 1);
+        d.rr0 = __shfl_sync(0xffffffffu, rr, 0);
+        d.rr1 = __shfl_sync(0xffffffffu, rr, 1);
+        d.ev0 = __shfl_sync(0xffffffffu, ev, 0);
+        d.ev1 = __shfl_sync(0xffffffffu, ev, 1);
         if (F.rain_kind == RAIN_STORM) {
             p.storm_on0 = p.t0 < F.storm_tstop;
             p.storm_on1 = p.t1 < F.storm_tstop;
-            d.sx0 = F.storm_x0 + F.storm_vx * p.t0;
-            d.sy0 = F.storm_y0 + F.storm_vy * p.t0;
-            d.sx1 = F.storm_x0 + F.storm_vx * p.t1;
-            d.sy1 = F.storm_y0 + F.storm_vy * p.t1;
+            d.sx0 = __shfl_sync(0xffffffffu, sx, 0);
+            d.sy0 = __shfl_sync(0xffffffffu, sy, 0);
+            d.sx1 = __shfl_sync(0xffffffffu, sx, 1);
+            d.sy1 = __shfl_sync(0xffffffffu, sy, 1);
         }
     }
     LaunchScalars<float> &f = p.f;
@@ -301,6 +315,21 @@ __device__ inline void clear_slot_accumulators(Clock &c) {
         for (int b = 0; b < kBuckets; b++) c.stepb[k][b] = 0.0;
     }
     for (int b = 0; b < kBuckets; b++) c.cmaxb[b] = 0ull;
+}
+
+// The same, by the lanes of one warp: lane b clears bucket b.
+__device__ inline void clear_slot_accumulators_warp(const int lane, Clock &c) {
+    if (lane < kBuckets) {
+        c.cmaxb[lane] = 0ull;
+        for (int k = 0; k < B_N; k++) c.stepb[k][lane] = 0.0;
+    }
+    if (lane == 0) {
+        c.cmax_bits = 0ull;
+        c.nonfinite = 0u;
+        c.status = 0u;
+        c.done_blocks = 0u;
+        for (int k = 0; k < B_N; k++) c.step[k] = 0.0;
+    }
 }
 
 __device__ inline void fold_totals(const Clock &ci, Clock &co) {
@@ -341,44 +370,59 @@ __device__ inline void accumulate_slot(Clock &co, int bucket, const double v[B_N
 
 // Finalises slot `co` once every contribution of the launch is in: sums the
 // buckets, folds the budgets, advances time, plans the next launch, and
-// clears slot `cn` for the launch after.  One thread.
-__device__ inline void finalize_slot(const Clock &ci, Clock &co, Clock &cn, const Plan &pl, const Control &ctl,
-                                     const GridDesc &G, const ForcingDesc &F) {
+// clears slot `cn` for the launch after.  Called by all 32 lanes of one
+// converged warp: lane b reads bucket b, and a shuffle tree (the same in
+// every lane) takes their maximum and sums; lane 0 writes the slot.
+__device__ inline void finalize_slot_warp(const int lane, const Clock &ci, Clock &co, Clock &cn, const Plan &pl,
+                                          const Control &ctl, const GridDesc &G, const ForcingDesc &F) {
     volatile Clock *cov = &co;
     unsigned long long cm = 0ull;
-    for (int b = 0; b < kBuckets; b++) {
-        const unsigned long long v = cov->cmaxb[b];
-        cm = v > cm ? v : cm;
+    double sum[B_N];
+    for (int k = 0; k < B_N; k++) sum[k] = 0.0;
+    if (lane < kBuckets) {
+        cm = cov->cmaxb[lane];
+        for (int k = 0; k < B_N; k++) sum[k] = cov->stepb[k][lane];
     }
-    for (int k = 0; k < B_N; k++) {
-        double sum = 0.0;
-        for (int b = 0; b < kBuckets; b++) sum += cov->stepb[k][b];
-        co.step[k] = sum;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long c2 = __shfl_xor_sync(0xffffffffu, cm, o);
+        cm = c2 > cm ? c2 : cm;
+#pragma unroll
+        for (int k = 0; k < B_N; k++) sum[k] += __shfl_xor_sync(0xffffffffu, sum[k], o);
     }
     const double t_new = (pl.t0 + pl.dt) + pl.dt;  // cu:1297, cu:1335
     const long long steps_new = ci.steps + 1;
-    fold_totals(ci, co);
-    co.cmax_bits = cm;
-    co.t = t_new;
-    co.dt = pl.dt;
-    co.steps = steps_new;
-    co.buf = 1 - ci.buf;
-    co.ran = 1;
-    co.nonfinite = cov->nonfinite | ci.nonfinite;
-    co.status = cov->status | ci.status;
-    co.plan = make_plan(t_new, cm, steps_new, ctl, G, F);
-    clear_slot_accumulators(cn);
+    const Plan np = make_plan_warp(lane, t_new, cm, steps_new, ctl, G, F);
+    if (lane == 0) {
+        for (int k = 0; k < B_N; k++) co.step[k] = sum[k];
+        fold_totals(ci, co);
+        co.cmax_bits = cm;
+        co.t = t_new;
+        co.dt = pl.dt;
+        co.steps = steps_new;
+        co.buf = 1 - ci.buf;
+        co.ran = 1;
+        co.nonfinite = cov->nonfinite | ci.nonfinite;
+        co.status = cov->status | ci.status;
+        co.plan = np;
+    }
+    clear_slot_accumulators_warp(lane, cn);
 }
 
-// Called by one thread of every CTA after its accumulate_slot; the last CTA
-// of the launch finalises the slot.  No CTA waits.
-__device__ inline void finish_cta(const Clock &ci, Clock &co, Clock &cn, const Plan &pl, const Control &ctl,
-                                  const GridDesc &G, const ForcingDesc &F) {
-    __threadfence();
-    const unsigned int ticket = atomicAdd(&co.done_blocks, 1u);
+// Called by all 32 lanes of one warp of every CTA after lane 0's
+// accumulate_slot; the last CTA of the launch finalises the slot.  No CTA
+// waits.
+__device__ inline void finish_cta_warp(const int lane, const Clock &ci, Clock &co, Clock &cn, const Plan &pl,
+                                       const Control &ctl, const GridDesc &G, const ForcingDesc &F) {
+    unsigned int ticket = 0u;
+    if (lane == 0) {
+        __threadfence();
+        ticket = atomicAdd(&co.done_blocks, 1u);
+    }
+    ticket = __shfl_sync(0xffffffffu, ticket, 0);
     if (ticket != gridDim.x * gridDim.y - 1) return;
     __threadfence();
-    finalize_slot(ci, co, cn, pl, ctl, G, F);
+    finalize_slot_warp(lane, ci, co, cn, pl, ctl, G, F);
 }
 
 // ---------------------------------------------------------------------------
@@ -961,33 +1005,36 @@ __global__ void __launch_bounds__(NT)
         for (int q = 0; q <= B_N; q++) s_red[wid][q] = vals[q];
     }
     __syncthreads();
-    if (tid != 0) return;
-    Real acc[B_N + 1];
+    if (tid >= 32) return;
+    if (tid == 0) {
+        Real acc[B_N + 1];
 #pragma unroll
-    for (int q = 0; q <= B_N; q++) acc[q] = s_red[0][q];
-    for (int w = 1; w < NW; w++) {
+        for (int q = 0; q <= B_N; q++) acc[q] = s_red[0][q];
+        for (int w = 1; w < NW; w++) {
 #pragma unroll
-        for (int q = 0; q < B_N; q++) acc[q] += s_red[w][q];
-        acc[B_N] = fmax(acc[B_N], s_red[w][B_N]);
+            for (int q = 0; q < B_N; q++) acc[q] += s_red[w][q];
+            acc[B_N] = fmax(acc[B_N], s_red[w][B_N]);
+        }
+        const double area = G.dx * G.dy;
+        const double scale = pl.d.dt2 * area;
+        double v[B_N];
+        v[B_RAIN] = (double)acc[B_RAIN] * scale;
+        v[B_SRC] = (double)acc[B_SRC] * scale;
+        v[B_EV] = (double)acc[B_EV] * scale;
+        v[B_OUT] = (double)acc[B_OUT] * pl.d.dt2 * G.dy;
+        v[B_CLAMP] = (double)acc[B_CLAMP] * area;
+        accumulate_slot(clk[slot_out], blockIdx.x % kBuckets, v, (double)acc[B_N], any_bad);
     }
-    const double area = G.dx * G.dy;
-    const double scale = pl.d.dt2 * area;
-    double v[B_N];
-    v[B_RAIN] = (double)acc[B_RAIN] * scale;
-    v[B_SRC] = (double)acc[B_SRC] * scale;
-    v[B_EV] = (double)acc[B_EV] * scale;
-    v[B_OUT] = (double)acc[B_OUT] * pl.d.dt2 * G.dy;
-    v[B_CLAMP] = (double)acc[B_CLAMP] * area;
-    accumulate_slot(clk[slot_out], blockIdx.x % kBuckets, v, (double)acc[B_N], any_bad);
-    finish_cta(ci, clk[slot_out], clk[slot_nx], pl, *ctl, G, F);
+    finish_cta_warp(lane, ci, clk[slot_out], clk[slot_nx], pl, *ctl, G, F);
 }
 
 // Plans the launch that will read slot `slot` (used when a run starts or its
-// control changes).  One thread.
+// control changes).  One warp.
 static __global__ void plan_kernel(const GridDesc G, const ForcingDesc F, Clock *__restrict__ clk,
                             const Control *__restrict__ ctl, const int slot) {
     Clock &c = clk[slot];
-    c.plan = make_plan(c.t, c.cmax_bits, c.steps, *ctl, G, F);
+    const Plan p = make_plan_warp((int)threadIdx.x, c.t, c.cmax_bits, c.steps, *ctl, G, F);
+    if (threadIdx.x == 0) c.plan = p;
 }
 
 }  // namespace sw2d

@@ -25,7 +25,7 @@
 //   * the next row's loads are issued before the current row's arithmetic.
 //
 // Budgets and the CFL bound are reduced per warp and then per CTA; the last
-// CTA of the launch finalises the clock slot (finish_cta).
+// CTA of the launch finalises the clock slot (finish_cta_warp).
 #pragma once
 
 #include "sw2d_stream_unit.cuh"
@@ -116,26 +116,28 @@ __global__ void __launch_bounds__(NWARP * 32, MINB)
         s_many[wid] = A.too_many_sources;
     }
     __syncthreads();
-    if (tid != 0) return;
-    double acc[B_N] = {0, 0, 0, 0, 0};
-    float cmb = 0.f;
-    bool anybad = false, many = false;
-    for (int w = 0; w < NWARP; w++) {
-        for (int q = 0; q < B_N; q++) acc[q] += (double)s_red[w][q];
-        cmb = fmaxf(cmb, s_red[w][B_N]);
-        anybad |= s_bad[w] != 0;
-        many |= s_many[w] != 0;
+    if (wid != 0) return;
+    if (lane == 0) {
+        double acc[B_N] = {0, 0, 0, 0, 0};
+        float cmb = 0.f;
+        bool anybad = false, many = false;
+        for (int w = 0; w < NWARP; w++) {
+            for (int q = 0; q < B_N; q++) acc[q] += (double)s_red[w][q];
+            cmb = fmaxf(cmb, s_red[w][B_N]);
+            anybad |= s_bad[w] != 0;
+            many |= s_many[w] != 0;
+        }
+        const double area = G.dx * G.dy, scale = ci.plan.d.dt2 * area;
+        double v[B_N];
+        v[B_RAIN] = acc[B_RAIN] * scale;
+        v[B_SRC] = acc[B_SRC] * scale;
+        v[B_EV] = acc[B_EV] * scale;
+        v[B_OUT] = acc[B_OUT] * ci.plan.d.dt2 * G.dy;
+        v[B_CLAMP] = acc[B_CLAMP] * area;
+        accumulate_slot(clk[slot_out], blockIdx.x % kBuckets, v, (double)cmb, anybad);
+        if (many) atomicOr(&clk[slot_out].status, (unsigned)ST_TOO_MANY_LOCAL_SOURCES);
     }
-    const double area = G.dx * G.dy, scale = ci.plan.d.dt2 * area;
-    double v[B_N];
-    v[B_RAIN] = acc[B_RAIN] * scale;
-    v[B_SRC] = acc[B_SRC] * scale;
-    v[B_EV] = acc[B_EV] * scale;
-    v[B_OUT] = acc[B_OUT] * ci.plan.d.dt2 * G.dy;
-    v[B_CLAMP] = acc[B_CLAMP] * area;
-    accumulate_slot(clk[slot_out], blockIdx.x % kBuckets, v, (double)cmb, anybad);
-    if (many) atomicOr(&clk[slot_out].status, (unsigned)ST_TOO_MANY_LOCAL_SOURCES);
-    finish_cta(ci, clk[slot_out], clk[slot_nx], ci.plan, *ctl, G, F);
+    finish_cta_warp(lane, ci, clk[slot_out], clk[slot_nx], ci.plan, *ctl, G, F);
 }
 
 }  // namespace sw2d
