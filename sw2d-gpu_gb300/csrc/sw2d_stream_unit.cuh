@@ -230,7 +230,8 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         return storm_amp * __expf(-(x * x + y * y) / storm_2s2);
     };
 
-    // row loads: rows R0-4 .. R1+2 and columns gj0-1 .. gj0+32 (the window and
+    // row loads: rows R0-4 .. R1+2 (the bed differences R0-4 .. R1+1) and
+    // columns gj0-1 .. gj0+32 (the window and
     // the neighbours loaded at its edges; gj0 >= -3, and the last window ends
     // 29 columns past the east wall) all lie inside the zero frame around the
     // domain, whose zeros are the inactive-cell and wall values, so no load
@@ -238,14 +239,13 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     float p_h, p_hw, p_hE, p_umE, p_vnE, p_dzx, p_dzy, p_n, p_um, p_vn, p_res;
     unsigned p_m;
     int gp = (R0 - 4) * pitch + gj;  // element offset of the next row to read (fields fit 32-bit offsets)
+    const int gp0 = gp;
     int lrow = R0 - 4;  // row of the next load
     auto load_row = [&]() {
         p_h = Hin[gp];
         p_hw = Hin[gp - 1];  // the west neighbour's depth, exact on lane 0 too
         p_res = lrow >= 3 ? Rin[gp - 3 * pitch] : 0.f;  // remainder of row lrow-3, used with this row
         lrow++;
-        p_dzx = DZX[gp];
-        p_dzy = DZY[gp];
         p_n = raster ? Nin[gp] : manning;
         p_m = (unsigned)Min[gp];
         p_um = Uin[gp];
@@ -258,7 +258,6 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
 
     // register rings: suffix = rows back from the row being read (r)
     float h1 = 0.f, h2 = 0.f, h3 = 0.f, hL1 = 0.f;
-    float dzx1 = 0.f, dzy1 = 0.f;  // bed differences of row r-1
     float n1 = manning, n2 = manning, nL1 = manning;
     float um1 = 0.f, um2 = 0.f, vn1 = 0.f, vn2 = 0.f;
     float uu_1 = 0.f, uu_2 = 0.f, uuL_1 = 0.f;
@@ -271,15 +270,23 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
 
     const int r_first = R0 - 4, r_last = R1 + 3;
     load_row();
+    p_dzx = 0.f;  // the bed differences of row r_first - 1 are not used
+    p_dzy = 0.f;
 #pragma unroll UNR
     for (int r = r_first; r < r_last; r++) {
         const float hE0 = p_hE, umE0 = p_umE, vnE0 = p_vnE;
-        const float h0 = p_h, hL0 = p_hw, dzx0 = p_dzx, dzy0 = p_dzy, n0 = p_n, um0 = p_um, vn0 = p_vn;
+        const float h0 = p_h, hL0 = p_hw, n0 = p_n, um0 = p_um, vn0 = p_vn;
         const float res3 = p_res;  // depth remainder of row r-3
         mb = (mb << 1) | p_m;
         const unsigned mL0 = __shfl_up_sync(0xffffffffu, p_m, 1);
         mLb = (mLb << 1) | mL0;
+        const float dzx1 = p_dzx, dzy1 = p_dzy;  // bed differences of row r-1
         if (r + 1 < r_last) load_row();  // prefetch the next row
+        // the bed differences are used one row after they are read, so they
+        // are read one row late (row r, for the next iteration) instead of
+        // passing through a register ring
+        p_dzx = DZX[(r - r_first) * pitch + gp0];
+        p_dzy = DZY[(r - r_first) * pitch + gp0];
 
         const float nL0 = raster ? shup(n0) : manning;
         // ---- row r: face velocities (cu:363-453) ----
@@ -425,7 +432,6 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
 
         // ---- advance the rings ----
         h3 = h2; h2 = h1; h1 = h0; hL1 = hL0;
-        dzx1 = dzx0; dzy1 = dzy0;
         n2 = n1; n1 = n0; nL1 = nL0;
         um2 = um1; um1 = um0; vn2 = vn1; vn1 = vn0;
         uu_2 = uu_1; uu_1 = uu_0; uuL_1 = uuL_0;
