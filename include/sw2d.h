@@ -168,6 +168,16 @@ int sw2d_set_rain_weights(sw2d_handle *h, const double *w);
  * where the depth is above EV_WL_min (cu:627-634).  n = 0 disables it. */
 int sw2d_set_evaporation(sw2d_handle *h, const double *series_mm, int32_t n, double dt_series);
 
+/* The evaporation series of the reference's energy-balance method, in mm per
+ * record interval, from n air temperatures [deg C] and global radiation
+ * values [W/m^2]: replaces gpu_evaporation_calc (cu:557-587) and the copy of
+ * its result to the host (cu:1242-1245).  A host computation (no handle, no
+ * device): the same operations in the same order, without FMA contraction;
+ * negative values become 0 (cu:583-585).  The result is what
+ * sw2d_set_evaporation takes, with dt_series = dtime. */
+int sw2d_evaporation_series(const double *temperature, const double *radiation, int32_t n, double albedo,
+                            double dtime, double *evap_mm);
+
 /* Point sources/sinks: cells[k] is the linear cell index i*cols+j of source
  * k; q is n_rec x n_src discharges [m^3/s] at interval dtoq, interpolated
  * with the reference's formula (stream_flow cu:532-546).  When two sources
@@ -276,12 +286,13 @@ const char *sw2d_batch_last_error(const sw2d_batch *b);
 
 /* Volume of water [m^3] on the active cells of a depth field that the
  * caller already holds on the device, for callers that cannot allocate
- * device memory when they need the mass-balance check: a host model that
- * captures its time loop into a CUDA graph in global capture mode (where
- * cudaMalloc fails), or one whose memory pool has reserved the whole GPU.
- * It allocates nothing: the partial sums live in a fixed 64 KiB array in
- * the library's device image (one per GPU that loads the library, held
- * until the process exits).  This entry point has no counterpart in the
+ * device memory when they need the mass-balance check: a host model whose
+ * own memory pool has reserved the whole GPU (a cudaMalloc there fails or
+ * makes the pool give memory back), or one that must not call the allocator
+ * inside its time loop (cudaMalloc and cudaFree can synchronise the device).
+ * It allocates nothing: the partial sums live in a fixed 64 KiB array in the
+ * library's device image (one per GPU that loads the library, held until
+ * the process exits).  This entry point has no counterpart in the
  * reference, which keeps no mass budget.
  *
  *   depth      device pointer, rows x cols float64 with a row pitch of
@@ -289,17 +300,18 @@ const char *sw2d_batch_last_error(const sw2d_batch *b);
  *   mask       device pointer with the same layout, 1 = active cell, or
  *              NULL when every cell counts
  *   cell_area  dx * dy [m^2]
- *   stream     cudaStream_t to run on (NULL = the legacy default stream);
- *              the call returns after the result is on the host
+ *   stream     cudaStream_t to run on (NULL = the legacy default stream)
  *
+ * The call waits for its stream: the volume is on the host when it returns.
  * Returns SW2D_ERR_INVALID_ARG for null pointers, pitch < cols, a
  * non-positive cell area, or rows * cols > SW2D_NOALLOC_MAX_CELLS.  The sum
  * is deterministic (fixed chunks of 8192 cells, Kahan inside each chunk,
- * chunks added in order).  The first call on a device looks up the scratch
- * array's device address; make that first call before any stream capture.
- * Every call reuses the same scratch array: calls that overlap on the GPU,
- * from different streams or threads, race and must be serialised by the
- * caller. */
+ * chunks added in order).  The first call in a CUDA context (one per device,
+ * and again after the context is destroyed and made anew) looks up the
+ * scratch array's device address; make that first call before any stream
+ * capture.  Every call reuses the same scratch array: calls that overlap on
+ * the GPU, from different streams or threads, race and must be serialised
+ * by the caller. */
 int sw2d_volume_noalloc(const double *depth, const uint8_t *mask, int32_t rows, int32_t cols, int32_t pitch,
                         double cell_area, void *stream, double *volume_out);
 

@@ -200,5 +200,22 @@ class Oracle:
         return float(lib().orc_next_dt(self._h, float(t_end)))
 
 
+def evaporation_series(temperature, radiation, albedo, dtime):
+    """The reference's evaporation per record [mm per record interval],
+    restated from gpu_evaporation_calc (SW2D-GPU.cu:557-587) in numpy float64
+    with the same operations in the same order: net radiation (1 - albedo)*Rg,
+    the ITS-90 water density polynomial, the latent heat of Henderson-Sellers
+    (1984), (Rs / (lv * pw)) * dtime * 1000, and 0 for negative values."""
+    T = np.asarray(temperature, dtype=np.float64)
+    Rg = np.asarray(radiation, dtype=np.float64)
+    Rs = (1 - albedo) * Rg
+    pw = (999.85308 + 6.32693 * (0.01) * T - 8.523829 * (0.001) * T * T + 6.943248 * (0.00001) * T * T * T
+          - 3.821216 * (0.0000001) * T * T * T * T)
+    a = T + 273.15
+    lv = ((a / (a - 33.91)) * (a / (a - 33.91))) * 1.91846 * 1000000
+    e = (Rs / (lv * pw)) * dtime * 1000.0
+    return np.where(e < 0, 0.0, e)
+
+
 def max_threads():
     return int(lib().orc_max_threads())

@@ -222,6 +222,20 @@ class RefRun:
                 "t": self.time, "steps": self.steps}
 
 
+def evaporation(mod: RefModule, albedo, temperature, radiation, dtime):
+    """The reference's gpu_evaporation_calc (cu:557-587) over a series, with
+    its launch shape; returns d_Evapo [mm per record interval]."""
+    t = mod.torch
+    T = t.from_numpy(np.ascontiguousarray(temperature, dtype=np.float64)).to("cuda")
+    Rg = t.from_numpy(np.ascontiguousarray(radiation, dtype=np.float64)).to("cuda")
+    n = T.numel()
+    Rs, pw, lv, ev = (t.zeros(n, dtype=t.float64, device="cuda") for _ in range(4))
+    P = lambda a: ("p", a.data_ptr())
+    mod.launch("gpu_evaporation_calc", n, ("d", albedo), P(T), P(Rg), P(Rs), P(pw), P(lv), P(ev), ("d", dtime),
+               ("i", n))
+    return ev.cpu().numpy()
+
+
 def reference_cell(rows, cols, qinx, qiny):
     """The reference's linear index for a point source at cell coordinates
     (qinx, qiny) counted from the lower-left corner (cu:542-545, Linux)."""

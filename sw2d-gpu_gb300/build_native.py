@@ -83,7 +83,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.replace(tmp, LIB)
     # the reference-format host driver: plain C++ on top of the C ABI
     cxx = shutil.which("g++") or "g++"
-    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I", os.path.join(ROOT, "include"),
+    # no FMA contraction (gcc contracts by default where the target has FMA,
+    # as the Arm hosts do): the driver's host arithmetic rounds the same on
+    # every machine
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
            os.path.join(CSRC, "sw2d_driver.cpp"), "-o", DRIVER + ".tmp", "-L", OUT_DIR, "-lsw2d",
            "-Wl,-rpath,$ORIGIN"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -607,6 +607,28 @@ int sw2d_set_evaporation(sw2d_handle *h, const double *series, int32_t n, double
     return SW2D_OK;
 }
 
+int sw2d_evaporation_series(const double *temperature, const double *radiation, int32_t n, double albedo,
+                            double dtime, double *evap_mm) {
+    if (n < 0 || (n > 0 && (!temperature || !radiation || !evap_mm)) || !(dtime > 0.0))
+        return SW2D_ERR_INVALID_ARG;
+    // energy-balance evaporation per record: net radiation, the ITS-90 water
+    // density polynomial (5-40 C) and the latent heat of vaporisation of
+    // Henderson-Sellers (1984), in the operation order of the reference
+    // (cu:557-587); this unit is compiled without FMA contraction, so every
+    // value rounds as there (and as in the reference built with --fmad=false)
+    for (int32_t i = 0; i < n; i++) {
+        const double t = temperature[i];
+        const double rs = (1 - albedo) * radiation[i];  // net radiation
+        const double pw = 999.85308 + 6.32693 * (0.01) * t - 8.523829 * (0.001) * t * t +
+                          6.943248 * (0.00001) * t * t * t - 3.821216 * (0.0000001) * t * t * t * t;
+        const double tk = t + 273.15;
+        const double lv = ((tk / (tk - 33.91)) * (tk / (tk - 33.91))) * 1.91846 * 1000000;
+        const double e = (rs / (lv * pw)) * dtime * 1000.0;  // mm per record interval
+        evap_mm[i] = e < 0 ? 0 : e;
+    }
+    return SW2D_OK;
+}
+
 int sw2d_set_point_sources(sw2d_handle *h, const int32_t *cells, int32_t n_src, const double *q, int32_t n_rec,
                            double dtoq) {
     if (!h) return SW2D_ERR_INVALID_ARG;

@@ -168,27 +168,6 @@ std::vector<std::pair<double, double>> read_coords(const std::string &path) {
 
 double c_round(double x) { return std::round(x); }  // half away from zero, as C round()
 
-// Evaporation per forcing record by the energy-balance method: net
-// radiation, water density (ITS-90 formulation) and latent heat of
-// vaporisation (Henderson-Sellers 1984), in mm per record interval; the
-// physics of the reference's gpu_evaporation_calc (cu:557-587), evaluated
-// on the host once per series.
-std::vector<double> evaporation_series(const std::vector<double> &T, const std::vector<double> &Rg, double albedo,
-                                       double dtime) {
-    std::vector<double> ev(T.size());
-    for (size_t i = 0; i < T.size(); i++) {
-        const double t = T[i];
-        const double rs = (1 - albedo) * Rg[i];
-        const double pw = 999.85308 + 6.32693 * (0.01) * t - 8.523829 * (0.001) * t * t +
-                          6.943248 * (0.00001) * t * t * t - 3.821216 * (0.0000001) * t * t * t * t;
-        const double tk = t + 273.15;
-        const double lv = ((tk / (tk - 33.91)) * (tk / (tk - 33.91))) * 1.91846 * 1000000;
-        double e = (rs / (lv * pw)) * dtime * 1000.0;
-        ev[i] = e < 0 ? 0 : e;
-    }
-    return ev;
-}
-
 int check(sw2d_handle *h, int st, const char *what) {
     if (st != SW2D_OK) {
         std::fprintf(stderr, "%s failed: %s (%s)\n", what, sw2d_status_string(st), h ? sw2d_last_error(h) : "");
@@ -265,7 +244,11 @@ int run_case(const Opts &o, const std::string &name) {
         const size_t n = std::min(T.size(), Rg.size());
         T.resize(n);
         Rg.resize(n);
-        evapo = evaporation_series(T, Rg, albedo, dtrain);
+        evapo.resize(n);
+        if (sw2d_evaporation_series(T.data(), Rg.data(), (int32_t)n, albedo, dtrain, evapo.data()) != SW2D_OK) {
+            std::printf("unknown file - evaporation.dat\n");
+            return 1;
+        }
     }
     // optional roughness raster (extension)
     Esri nman;

@@ -3,12 +3,13 @@
 //
 // sw2d_get_budget sums the depth field with volume_kernel into a partial-sum
 // buffer the handle allocated with cudaMalloc.  Some callers cannot allocate
-// at the point where they need that check: a host model that runs its time
-// loop while capturing a CUDA graph in global capture mode (where cudaMalloc
-// is an error), or an application whose memory pool has already reserved the
-// whole device.  sw2d_volume_noalloc runs the same kind of reduction on
-// device arrays the caller passes in, keeping its partial sums in a fixed
-// array that is part of this library's device image instead.
+// at the point where they need that check: a host model whose own memory
+// pool has already reserved the whole device (a cudaMalloc there fails, or
+// makes the pool give memory back), or one that must not call the allocator
+// inside its time loop (cudaMalloc and cudaFree can synchronise the device).
+// sw2d_volume_noalloc runs the same kind of reduction on device arrays the
+// caller passes in, keeping its partial sums in a fixed array that is part of
+// this library's device image instead.
 //
 // Scratch: g_volume_scratch, kNoallocMaxChunks + 1 doubles (64 KiB), resident
 // on every GPU that loads the library until the process exits.  Chunk b holds
@@ -16,6 +17,13 @@
 // the last element receives the total.  Every call overwrites the partials it
 // uses, so nothing has to start at zero; calls that overlap on the GPU
 // (different streams, or different host threads) share the array and race.
+//
+// Set-up: host code cannot use the array's name as a device address, so the
+// first call in a CUDA context (per device, and again after the context was
+// destroyed and made anew, e.g. by cudaDeviceReset) looks the address up with
+// cudaGetSymbolAddress, with that device current, and keeps it for the
+// context's lifetime.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -77,23 +85,64 @@ __global__ void noalloc_volume_total(double *__restrict__ partial, int n) {
 }
 
 std::mutex g_setup_mutex;
-double *g_scratch_ptr[kMaxDevices] = {nullptr};
 
-// Device address of the scratch array on the current device, looked up once
-// per device (cudaGetSymbolAddress with that device current).
+// The scratch address of each device, with the context it is valid in.
+struct ScratchEntry {
+    unsigned long long ctx_id;  // cuCtxGetId of the context (never reused in a process); 0 = none
+    double *ptr;
+};
+ScratchEntry g_scratch[kMaxDevices] = {};
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+// The identity of the current context through the driver's entry points (no
+// link against the driver library); 0 when there is none or it cannot be
+// told.
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        cudaDriverEntryPointQueryResult q1, q2;
+        void *f1 = nullptr, *f2 = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q2 == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+            get_id = reinterpret_cast<CtxGetIdFn>(f2);
+        }
+        looked_up = true;
+    }
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch array in the current context: looked up once
+// per context (cudaGetSymbolAddress with the device current) and kept.
 cudaError_t scratch_for_current_device(double **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (g_scratch_ptr[dev] == nullptr) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_volume_scratch);
-        if (e != cudaSuccess) return e;
-        g_scratch_ptr[dev] = static_cast<double *>(p);
+    const unsigned long long id = current_context_id();
+    if (id != 0 && g_scratch[dev].ctx_id == id && g_scratch[dev].ptr != nullptr) {
+        *out = g_scratch[dev].ptr;
+        return cudaSuccess;
     }
-    *out = g_scratch_ptr[dev];
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_volume_scratch);  // also makes the device's primary context current
+    if (e != cudaSuccess) return e;
+    // keyed on the context now current; when it cannot be told, nothing is
+    // kept and the next call looks the address up again
+    g_scratch[dev].ctx_id = current_context_id();
+    g_scratch[dev].ptr = g_scratch[dev].ctx_id != 0 ? static_cast<double *>(p) : nullptr;
+    *out = static_cast<double *>(p);
     return cudaSuccess;
 }
 
@@ -108,6 +157,7 @@ extern "C" int sw2d_volume_noalloc(const double *depth, const uint8_t *mask, int
     double *scratch = nullptr;
     if (scratch_for_current_device(&scratch) != cudaSuccess) return SW2D_ERR_CUDA;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    (void)cudaGetLastError();  // an earlier, unrelated launch error is not this call's
     const int nchunks = (int)((ncells + kNoallocChunk - 1) / kNoallocChunk);
     noalloc_volume_chunks<<<nchunks, kNoallocThreads, 0, st>>>(depth, mask, rows, cols, pitch, ncells, scratch);
     if (cudaGetLastError() != cudaSuccess) return SW2D_ERR_CUDA;

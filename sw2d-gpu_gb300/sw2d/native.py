@@ -74,6 +74,7 @@ _SIGS = {
     "sw2d_set_rain": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_double]),
     "sw2d_set_storm": (C.c_int, [C.c_void_p] + [C.c_double] * 7),
     "sw2d_set_evaporation": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_double]),
+    "sw2d_evaporation_series": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_void_p]),
     "sw2d_set_point_sources": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_double]),
     "sw2d_advance": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.POINTER(C.c_int64)]),
     "sw2d_get_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
@@ -142,6 +143,20 @@ def _f64(a, shape=None):
     if shape is not None and a.shape != shape:
         a = a.reshape(shape)
     return a
+
+
+def evaporation_series(temperature, radiation, albedo, dtime):
+    """The reference's energy-balance evaporation [mm per record interval] from air temperatures [deg C]
+    and global radiation [W/m^2] (host computation, sw2d_evaporation_series)."""
+    t = _f64(np.atleast_1d(temperature))
+    r = _f64(np.atleast_1d(radiation))
+    if t.shape != r.shape:
+        raise ValueError("temperature and radiation series differ in length")
+    out = np.empty_like(t)
+    st = load().sw2d_evaporation_series(_p(t), _p(r), t.size, float(albedo), float(dtime), _p(out))
+    if st != OK:
+        raise SW2DError(st, "sw2d_evaporation_series")
+    return out
 
 
 def default_config(**kw) -> Config:
@@ -237,7 +252,8 @@ class Solver:
         self._check(load().sw2d_set_rain_weights(self._h, _p(w)), "sw2d_set_rain_weights")
 
     def set_evaporation(self, series=None, dt_series=1.0):
-        """Evaporation series [m/s] every dt_series seconds, applied where the depth exceeds cfg.EV_WL_min."""
+        """Evaporation series [mm per interval] every dt_series seconds (the reference's evaporation_load),
+        applied where the depth exceeds cfg.EV_WL_min."""
         s = _f64(np.atleast_1d(series)) if series is not None else None
         n = 0 if s is None else s.size
         self._check(load().sw2d_set_evaporation(self._h, _p(s), n, float(dt_series)), "sw2d_set_evaporation")
