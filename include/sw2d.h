@@ -253,7 +253,8 @@ typedef struct {
     int32_t strip_h;       /* rows per warp, 0 = by scenario size */
     int64_t max_bytes;     /* device budget for scenario data, 0 = none */
     int32_t chunk;         /* launches per CUDA-graph replay (multiple of 3) */
-    int32_t reserved[3];
+    int32_t variant;       /* build of the batched kernel, 0..2 (0 = default; the autotuner's choice) */
+    int32_t reserved[2];
 } sw2d_batch_config;
 
 int sw2d_batch_config_init(sw2d_batch_config *cfg);

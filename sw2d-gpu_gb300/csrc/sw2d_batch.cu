@@ -24,8 +24,12 @@ using namespace sw2d;
 
 namespace {
 
-constexpr int kBatchWarps = 8;  // the streaming kernel's default build (8 warps, 2 CTAs per SM)
-constexpr int kBatchMinBlocks = 2;
+// Builds of the batched kernel the autotuner chooses from: (id, warps per
+// CTA, minimum resident CTAs per SM -- the register budget --, unrolling of
+// the row loop).  Build 0 is the default: 8 warps and 2 CTAs per SM leave
+// room for the queue state without spilling.
+#define SW2D_BATCH_VARIANTS(X) X(0, 8, 2, 1) X(1, 8, 2, 2) X(2, 4, 4, 1)
+constexpr int kBatchVariants = 3;
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -84,8 +88,26 @@ cudaError_t launch_batch(sw2d_batch *b, int slot) {
     B.scen = b->d_scen;
     B.units = b->d_units;
     B.hdr = b->d_hdr;
-    batch_step_kernel<kBatchWarps, kBatchMinBlocks><<<b->grid, kBatchWarps * 32, 0, b->stream>>>(B, slot);
-    return cudaGetLastError();
+#define SW2D_BL(id, nw, mb, un)                                                                 \
+    if (b->cfg.variant == id) {                                                                 \
+        batch_step_kernel<nw, mb, un><<<b->grid, nw * 32, 0, b->stream>>>(B, slot);             \
+        return cudaGetLastError();                                                              \
+    }
+    SW2D_BATCH_VARIANTS(SW2D_BL)
+#undef SW2D_BL
+    return cudaErrorInvalidValue;
+}
+
+// Resident CTAs per SM of a build (its grid is that many per SM), 0 on error.
+int batch_ctas_per_sm(int variant) {
+    int n = 0;
+#define SW2D_BO(id, nw, mb, un)                                                                              \
+    if (variant == id &&                                                                                     \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<nw, mb, un>, nw * 32, 0) != cudaSuccess) \
+        n = 0;
+    SW2D_BATCH_VARIANTS(SW2D_BO)
+#undef SW2D_BO
+    return n;
 }
 
 int capture(sw2d_batch *b, int parity) {
@@ -174,7 +196,8 @@ int sw2d_batch_scenario_bytes(const sw2d_config *cfg, int32_t n_rain, int32_t wi
 int sw2d_batch_create(const sw2d_batch_config *cfg, sw2d_batch **out) {
     if (!cfg || !out) return SW2D_ERR_INVALID_ARG;
     *out = nullptr;
-    if (cfg->max_scenarios < 1 || cfg->max_units < 1 || cfg->chunk < 3 || cfg->chunk % 3 != 0 || cfg->strip_h < 0)
+    if (cfg->max_scenarios < 1 || cfg->max_units < 1 || cfg->chunk < 3 || cfg->chunk % 3 != 0 || cfg->strip_h < 0 ||
+        cfg->variant < 0 || cfg->variant >= kBatchVariants)
         return SW2D_ERR_INVALID_ARG;
     sw2d_batch *b = new sw2d_batch();
     b->cfg = *cfg;
@@ -198,12 +221,10 @@ int sw2d_batch_create(const sw2d_batch_config *cfg, sw2d_batch **out) {
     cudaMemset(b->d_scen, 0, (size_t)cfg->max_scenarios * sizeof(ScenarioDev));
     cudaMemset(b->d_status, 0, (size_t)cfg->max_scenarios * sizeof(ScenarioStatus));
     b->scen.resize(cfg->max_scenarios);
-    int sms = 0, per_sm = 0;
+    int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg->device);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_step_kernel<kBatchWarps, kBatchMinBlocks>,
-                                                      kBatchWarps * 32, 0) != cudaSuccess ||
-        per_sm < 1)
-        per_sm = 1;
+    int per_sm = batch_ctas_per_sm(cfg->variant);
+    if (per_sm < 1) per_sm = 1;
     b->grid = (sms > 0 ? sms : 152) * per_sm;
     if (cudaDeviceSynchronize() != cudaSuccess) return bail(SW2D_ERR_CUDA);
     *out = b;

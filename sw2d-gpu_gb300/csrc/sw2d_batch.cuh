@@ -65,7 +65,7 @@ __device__ inline void write_status(const Clock &c, ScenarioStatus *st) {
     st->status = c.status;
 }
 
-template <int NWARP, int MINB>
+template <int NWARP, int MINB, int UNR>
 __global__ void __launch_bounds__(NWARP * 32, MINB) batch_step_kernel(const BatchDev B, const int slot) {
     __shared__ int s_sr[NWARP][kStreamMaxSrc], s_sc[NWARP][kStreamMaxSrc];
     __shared__ float s_q0[NWARP][kStreamMaxSrc], s_q1[NWARP][kStreamMaxSrc];
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(NWARP * 32, MINB) batch_step_kernel(const Batc
             const int ct = ue.y % S.tiles_w, rs = ue.y / S.tiles_w;
             // batched scenarios take neither a storm nor point sources nor rain
             // factors (sw2d_batch_add accepts none), so the uniform-forcing unit
-            stream_unit<1, false, false>(V, ct, rs, S.strip_h, lane, s_sr[wid], s_sc[wid], s_q0[wid], s_q1[wid], A);
+            stream_unit<UNR, false, false>(V, ct, rs, S.strip_h, lane, s_sr[wid], s_sc[wid], s_q0[wid], s_q1[wid], A);
             warp_reduce_acc(A);
             if (lane == 0) {
                 const double area = S.G.dx * S.G.dy, scale = ci.plan.d.dt2 * area;

@@ -1,14 +1,19 @@
-"""Autotuner for the FP32 streaming kernel: tile shape and launches per sync.
+"""Autotuner for the FP32 kernels: tile shape, kernel build, launches per sync.
 
 For a grid-size class it times every candidate (strip height, kernel build)
-on a wet synthetic catchment of that size and keeps the fastest, then times
-the CUDA-graph chunk (iterations replayed between host synchronisations) for
-batched runs.  Results are cached in a JSON file keyed by GPU name and size
-class, so a tuning run is paid once per machine.
+of the single-scenario streaming kernel on a wet synthetic catchment of that
+size and keeps the fastest; for batches it times the builds of the batched
+kernel with the CUDA-graph chunk (iterations replayed between host
+synchronisations) on a small ensemble.  Results are cached in a JSON file
+keyed by GPU name and size class (SW2D_AUTOTUNE_CACHE names the file), so a
+tuning run is paid once per machine.  Solver(**kw) and Batch(**kw) take the
+cached choice when the caller leaves the decomposition to the library
+(SW2D_AUTOTUNE=0 turns that off).
 
     from sw2d import autotune
-    best = autotune.tune(2048, 2048)          # {"strip_h": 48, "variant": 0, ...}
+    best = autotune.tune(2048, 2048)          # {"strip_h": 52, "variant": 0, ...}
     cfg = autotune.apply(cfg)                 # fills strip_h/variant from the cache
+    autotune.tune_batch()                     # {"variant": 0, "chunk": 24, ...}
 """
 from __future__ import annotations
 
@@ -39,9 +44,19 @@ def wave_strips(rows: int, cols: int, sms: int = 152, waves=(1, 2, 3, 4), warps_
     return sorted({max(16, -(-rows // max(1, (w * sms * per) // tiles_w))) for w in waves for per in warps_per_sm})
 
 
+BATCH_VARIANTS = (0, 1, 2)
+BATCH_CLASS = "batch"
+
+
 def default_cache_path() -> str:
+    if os.environ.get("SW2D_AUTOTUNE_CACHE"):
+        return os.environ["SW2D_AUTOTUNE_CACHE"]
     base = os.environ.get("XDG_CACHE_HOME", os.path.join(os.path.expanduser("~"), ".cache"))
     return os.path.join(base, "sw2d", "autotune.json")
+
+
+def enabled() -> bool:
+    return os.environ.get("SW2D_AUTOTUNE", "1") != "0"
 
 
 def size_class(rows: int, cols: int) -> str:
@@ -157,6 +172,56 @@ def apply(cfg, cache: Optional[Cache] = None, device: int = 0):
         cfg.strip_h = int(hit["strip_h"])
         cfg.variant = int(hit["variant"])
     return cfg
+
+
+def _batch_timer(device, count, launches):
+    import sw2d
+    from sw2d import scenarios as S
+    bank = S.TerrainBank(size=1024, dx=5.0, seed=3)
+    ens = S.ensemble(bank, count=count, sides=(128, 256, 512, 1024), seed=4)
+
+    def timer(c):
+        b = sw2d.Batch(sw2d.batch_config(device=device, chunk=c["chunk"], variant=c["variant"],
+                                         max_scenarios=count + 1))
+        try:
+            for e in ens:
+                cfg = sw2d.default_config(rows=e["side"], cols=e["side"], dx=5.0, dy=5.0, precision=sw2d.PREC_F32,
+                                          dt_mode=sw2d.DT_CFL, dt=1.0, cfl=0.5, south_open=1, device=device)
+                b.add(cfg, e["z"], np.full((e["side"], e["side"]), 0.005), manning=e["n"],
+                      rain_kind=sw2d.RAIN_LINEAR, rain=e["rain"], rain_dt=e["rain_dt"], t_end=1e9)
+            n = max(launches, c["chunk"])
+            b.advance(c["chunk"])
+            b.advance(c["chunk"] * 2)  # warm-up, including the graph builds
+            t0 = time.perf_counter()
+            b.advance(n)
+            return (time.perf_counter() - t0) / n
+        finally:
+            b.close()
+    return timer
+
+
+def tune_batch(device: int = 0, cache: Optional[Cache] = None, variants=BATCH_VARIANTS, chunks=(12, 24, 48),
+               count: int = 24, launches: int = 96, force: bool = False) -> dict:
+    """Best (batched-kernel build, graph chunk) on a small wet ensemble (cached)."""
+    cache = cache or Cache()
+    gpu = f"{gpu_name(device)}|{TABLE_VERSION}"
+    hit = cache.get(gpu, BATCH_CLASS)
+    if hit and not force:
+        return hit
+    cands = [{"variant": v, "chunk": ch} for v in variants for ch in chunks]
+    best, table = search(cands, _batch_timer(device, count, launches))
+    entry = {**best, "timings": table}
+    cache.put(gpu, BATCH_CLASS, entry)
+    return entry
+
+
+def apply_batch(bcfg, cache: Optional[Cache] = None):
+    """Fills bcfg.variant / bcfg.chunk from the cache; returns bcfg."""
+    hit = (cache or Cache()).get(f"{gpu_name(bcfg.device)}|{TABLE_VERSION}", BATCH_CLASS)
+    if hit:
+        bcfg.variant = int(hit["variant"])
+        bcfg.chunk = int(hit["chunk"])
+    return bcfg
 
 
 def tune_chunk(batch_runner: Callable[[int], float], chunks=CHUNKS) -> dict:

@@ -51,7 +51,7 @@ class Budget(C.Structure):
 class BatchConfig(C.Structure):
     _fields_ = [
         ("device", C.c_int32), ("max_scenarios", C.c_int32), ("max_units", C.c_int32), ("strip_h", C.c_int32),
-        ("max_bytes", C.c_int64), ("chunk", C.c_int32), ("reserved", C.c_int32 * 3),
+        ("max_bytes", C.c_int64), ("chunk", C.c_int32), ("variant", C.c_int32), ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -181,8 +181,15 @@ class Solver:
     """One scenario on the GPU, owned through a C-ABI handle."""
 
     def __init__(self, cfg: Config | None = None, **kw):
+        """Creates the handle from a Config or from its fields as keywords.  With keywords that leave the
+        decomposition to the library (no strip_h, variant or kernel) an FP32 handle takes the autotuner's
+        cached choice for its size class on this GPU, when there is one (sw2d.autotune)."""
         L = load()
         self.cfg = cfg if cfg is not None else default_config(**kw)
+        if cfg is None and not ({"strip_h", "variant", "kernel"} & set(kw)) and self.cfg.precision == PREC_F32:
+            from . import autotune
+            if autotune.enabled():
+                autotune.apply(self.cfg, device=self.cfg.device)
         h = C.c_void_p()
         st = L.sw2d_create(C.byref(self.cfg), C.byref(h))
         if st != OK:
@@ -361,8 +368,15 @@ class Batch:
     """Many FP32 scenarios advanced together on one GPU (C-ABI sw2d_batch_*)."""
 
     def __init__(self, cfg: BatchConfig | None = None, **kw):
+        """Creates the batch from a BatchConfig or from its fields as keywords.  With keywords that leave the
+        kernel build and graph chunk to the library (no variant or chunk) the batch takes the autotuner's
+        cached choice on this GPU, when there is one (sw2d.autotune.tune_batch)."""
         L = load()
         self.cfg = cfg if cfg is not None else batch_config(**kw)
+        if cfg is None and not ({"variant", "chunk"} & set(kw)):
+            from . import autotune
+            if autotune.enabled():
+                autotune.apply_batch(self.cfg)
         h = C.c_void_p()
         st = L.sw2d_batch_create(C.byref(self.cfg), C.byref(h))
         if st != OK:

@@ -58,3 +58,53 @@ def test_wave_strips_include_the_library_choice():
     # more waves give shorter strips, never below 16 rows
     many = autotune.wave_strips(2048, 2048, sms=152)
     assert min(many) >= 16 and 52 in many and max(many) >= 52
+
+
+@pytest.mark.gpu
+def test_solver_takes_the_cached_choice(sw2d_mod, tmp_path, monkeypatch):
+    """A cache entry for the size class changes the decomposition the library
+    reports (sw2d_describe) for a handle created without an explicit one;
+    an explicit strip height, or SW2D_AUTOTUNE=0, keeps the caller's."""
+    from sw2d import autotune
+    monkeypatch.setenv("SW2D_AUTOTUNE_CACHE", str(tmp_path / "t.json"))
+    kw = dict(rows=256, cols=256, precision=sw2d_mod.PREC_F32, dt_mode=sw2d_mod.DT_CFL)
+    with sw2d_mod.Solver(**kw) as g:
+        before = g.describe()
+    autotune.Cache().put(f"{autotune.gpu_name(0)}|{autotune.TABLE_VERSION}", autotune.size_class(256, 256),
+                         {"strip_h": 24, "variant": 3})
+    with sw2d_mod.Solver(**kw) as g:
+        tuned = g.describe()
+    assert "stream_step_kernel<8,2,1>" in tuned and "strip_h=24" in tuned and tuned != before
+    with sw2d_mod.Solver(strip_h=32, **kw) as g:
+        assert "strip_h=32" in g.describe()
+    monkeypatch.setenv("SW2D_AUTOTUNE", "0")
+    with sw2d_mod.Solver(**kw) as g:
+        assert g.describe() == before
+
+
+@pytest.mark.gpu
+def test_batch_tuning_picks_a_build_and_chunk(sw2d_mod, tmp_path, monkeypatch):
+    """tune_batch times builds of the batched kernel with graph chunks and a
+    Batch created without them takes the choice; every build advances a
+    scenario to the same bits (the arithmetic does not depend on the build)."""
+    import numpy as np
+    from sw2d import autotune
+    from sw2d import scenarios as S
+    monkeypatch.setenv("SW2D_AUTOTUNE_CACHE", str(tmp_path / "t.json"))
+    best = autotune.tune_batch(variants=(0, 2), chunks=(6, 12), count=4, launches=24)
+    assert best["variant"] in (0, 2) and best["chunk"] in (6, 12) and len(best["timings"]) == 4
+    b = sw2d_mod.Batch(max_scenarios=4)
+    assert (b.cfg.variant, b.cfg.chunk) == (best["variant"], best["chunk"])
+    b.close()
+    s = S.catchment(96, dx=5.0, seed=2)
+    depth = {}
+    for v in (0, 1, 2):
+        with sw2d_mod.Batch(variant=v, chunk=6, max_scenarios=2) as bt:
+            cfg = sw2d_mod.default_config(rows=96, cols=96, dx=5.0, dy=5.0, precision=sw2d_mod.PREC_F32,
+                                          dt_mode=sw2d_mod.DT_CFL, dt=1.0, south_open=1)
+            sid = bt.add(cfg, s["z"], np.full((96, 96), 0.01), manning=s["n"], rain_kind=sw2d_mod.RAIN_STEP,
+                         rain=np.array([60.0]), rain_dt=3600.0, t_end=120.0)
+            while bt.advance(12):
+                pass
+            depth[v] = bt.field(sid)
+    assert np.array_equal(depth[0], depth[1]) and np.array_equal(depth[0], depth[2])
