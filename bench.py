@@ -48,6 +48,10 @@ B_ALG_F32 = 32           # algorithmic bytes per cell-update: read h,um,vn,z,n +
 B_ALG_F64 = 64
 METRIC = "cell-updates/s"
 ACC_WINDOW_S = 60.0      # simulated seconds of the FP32-vs-FP64 accuracy leg
+LARGE = 8192             # the large-single-domain configuration: 8192^2, dx 2 m, n 0.05, moving storm
+LARGE_DX = 2.0
+LARGE_SPINUP_T = 1800.0  # the storm centre has crossed most of the diagonal by then
+B_ALG_F32_SCALAR_N = 28  # algorithmic bytes per cell-update with a scalar Manning n
 
 
 def log(*a):
@@ -161,9 +165,22 @@ def run_ours(args):
     dev = local
     torch.cuda.set_device(dev)
     sw2d.load()
-    from sw2d import replicas
+    from sw2d import autotune, replicas
     s = scenario(replicas.rank_seed(SEED, rank))
     active = int(np.count_nonzero(s["z"] != -9999.0))
+
+    # ---- autotuning (untimed): strip height and kernel build of the
+    # single-domain kernel for this size class, build and graph chunk of the
+    # batched kernel; the solvers and batches below take the choices.  The
+    # cache lives beside the built library, so a fresh build tunes afresh.
+    os.environ.setdefault("SW2D_AUTOTUNE_CACHE", os.path.join(ROOT, "sw2d-gpu_gb300", "_build", "autotune.json"))
+    t_tune = time.perf_counter()
+    tuned = autotune.tune(SIZE, SIZE, device=dev, iters=CHUNK, strips=())
+    tuned_b = autotune.tune_batch(device=dev) if (args.batched or args.served) else {}
+    tune_s = time.perf_counter() - t_tune
+    log(f"[rank {rank}] autotune: strip_h={tuned['strip_h']} variant={tuned['variant']} "
+        f"batch={tuned_b.get('variant')}/{tuned_b.get('chunk')} ({tune_s:.1f}s, "
+        f"{len(tuned.get('timings', []))} + {len(tuned_b.get('timings', []))} candidates)")
 
     g = make_solver(sw2d, s, sw2d.PREC_F32, dev)
     g.set_state(s["h0"])
@@ -259,6 +276,9 @@ def run_ours(args):
     d2h = (clock_b + partials_b) + k_e2e * (clock_b + partials_b) + SIZE * SIZE * 8
     assert np.isfinite(out_h).all()
 
+    # ---- large single domain (extra key) -------------------------------------
+    large = run_large(sw2d, dev, args, peak) if args.large else None
+
     # ---- batched ensemble and served stream (extra keys) --------------------
     batched = run_batched(sw2d, dev, args, rank, ws) if args.batched else None
     served = run_served(sw2d, dev, args) if args.served else None
@@ -281,7 +301,11 @@ def run_ours(args):
                                    "state spun up to t=1800 s; FP32 state, FP64 budgets",
                        "grid": [SIZE, SIZE], "active_cells": active, "iterations_per_step": CHUNK,
                        "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{ws}",
-                       "seed": SEED},
+                       "seed": SEED,
+                       "autotuned": {"strip_h": tuned["strip_h"], "variant": tuned["variant"], "kernel": kernel_desc,
+                                     "batch_variant": tuned_b.get("variant"), "batch_chunk": tuned_b.get("chunk"),
+                                     "steps_per_launch": 1, "tuning_s": tune_s,
+                                     "candidates": len(tuned.get("timings", [])) + len(tuned_b.get("timings", []))}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": (tpc * active if tpc is not None else None),
@@ -296,6 +320,7 @@ def run_ours(args):
             "fp64_plain": {"value": v64, "unit": "cell-updates/s", "speedup_f32_over_f64": value / ws / v64},
             "volume_rel_error": vol_err,
             "accuracy_vs_fp64": accuracy,
+            "large_domain": large,
             "batched": batched,
             "served": served,
         }
@@ -357,16 +382,16 @@ def run_batched(sw2d, dev, args, rank=0, ws=1):
     """The batched-ensemble configuration: 256 scenarios, sides uniform over
     {128, 256, 512, 1024}, triangular hyetographs, Manning scaling, horizon =
     rain duration + 1800 s; all advanced together until the last one ends.
-    The serial FP64 plain path is timed on one scenario per size class and
-    extrapolated with the ensemble's own iteration counts.  Under torchrun
-    each rank advances its contiguous share of the ensemble."""
+    The serial FP64 plain path is measured on whole scenarios of every size
+    class (fp64_alone).  Under torchrun each rank advances its contiguous
+    share of the ensemble."""
     import torch
     from sw2d import replicas
     from sw2d import scenarios as S
     ens_all = S.ensemble(terrain_bank(), count=args.batch_count, seed=SEED + 11)
     ens = [ens_all[k] for k in replicas.shard(len(ens_all), rank, ws)]
     t0 = time.perf_counter()
-    b = sw2d.Batch(device=dev, chunk=24, max_scenarios=len(ens) + 8)
+    b = sw2d.Batch(device=dev, max_scenarios=len(ens) + 8)  # build and chunk: the autotuner's
     ids = [b.add(scen_cfg(sw2d, e["side"], device=dev), e["z"], e["h0"], manning=e["n"],
                  rain_kind=sw2d.RAIN_LINEAR, rain=e["rain"], rain_dt=e["rain_dt"], t_end=e["t_end"]) for e in ens]
     t_admit = time.perf_counter() - t0
@@ -384,26 +409,33 @@ def run_batched(sw2d, dev, args, rank=0, ws=1):
     status = b.poll()
     cu = sum(e["side"] * e["side"] * status[i]["steps"] for e, i in zip(ens, ids))
     launches = b.launch_count() - launches0
-    # error against FP64: one scenario per side class up to 512, rerun alone
-    # through the FP64 plain path to the same end time
-    errors = []
-    for side in sorted({e["side"] for e in ens if e["side"] <= 512}):
-        k = next(j for j, e in enumerate(ens) if e["side"] == side)
-        e = ens[k]
-        g = sw2d.Solver(scen_cfg(sw2d, side, precision=sw2d.PREC_F64, device=dev))
-        g.set_static(e["z"], e["n"])
-        g.set_state(e["h0"])
-        g.set_rain(sw2d.RAIN_LINEAR, e["rain"], e["rain_dt"])
-        g.advance(10 ** 9, t_end=e["t_end"])
-        err = depth_error(g.depth(), b.field(ids[k], sw2d.FIELD_DEPTH))
-        err["side"] = side
-        errors.append(err)
-        g.close()
+    # The serial baseline, measured: the FP64 plain single-scenario path runs
+    # `batch_fp64_per_class` whole scenarios of each size class one after the
+    # other, each alone to its own end time (set-up, advance and the depth
+    # download timed); each result is also the FP64 reference of the batched
+    # FP32 result of the same scenario.  The serial time of the whole ensemble
+    # is each class's mean measured time times the class's scenario count.
+    by_side = {}
+    for k, e in enumerate(ens):
+        by_side.setdefault(e["side"], []).append(k)
+    measured, errors = {}, []
+    for side in sorted(by_side):
+        errs = []
+        for k in by_side[side][:args.batch_fp64_per_class]:
+            sec, h64, _ = fp64_alone(sw2d, dev, ens[k])
+            measured.setdefault(side, []).append(sec)
+            errs.append(depth_error(h64, b.field(ids[k], sw2d.FIELD_DEPTH)))
+        errors.append({"side": side, "scenarios": len(errs),
+                       "max_abs_dh_m": max(x["max_abs_dh_m"] for x in errs),
+                       "p9999_abs_dh_m": max(x["p9999_abs_dh_m"] for x in errs),
+                       "flooded_area_rel_diff": max(x["flooded_area_rel_diff"] for x in errs)})
     b.close()
-    # serial FP64 plain path, per size class
+    serial64_meas = sum(statistics.mean(measured[side]) * len(by_side[side]) for side in by_side)
+    # the earlier estimate beside it: the FP64 rate on a 5 mm film per size
+    # class times the ensemble's own FP32 iteration counts
     rate64 = {}
-    for side in sorted({e["side"] for e in ens}):
-        e = next(x for x in ens if x["side"] == side)
+    for side in sorted(by_side):
+        e = ens[by_side[side][0]]
         g = sw2d.Solver(scen_cfg(sw2d, side, precision=sw2d.PREC_F64, device=dev))
         g.set_static(e["z"], e["n"])
         g.set_state(np.full((side, side), 0.005))
@@ -420,12 +452,109 @@ def run_batched(sw2d, dev, args, rank=0, ws=1):
     cu_all, gpu_s_all = replicas.job_totals(cu, gpu_s, device=dev_name)
     n_all, wall_all = replicas.job_totals(len(ens), wall, device=dev_name)
     serial_all, _ = replicas.job_totals(serial64_s, 0.0, device=dev_name)
+    serial_meas_all, _ = replicas.job_totals(serial64_meas, 0.0, device=dev_name)
     return {"scenarios": int(n_all), "cells": int(sum(e["side"] ** 2 for e in ens_all)), "cell_updates": int(cu_all),
             "gpu_s": gpu_s_all, "wall_s_incl_admission": wall_all, "admission_s": t_admit, "launches": int(launches),
             "cell_updates_per_s": cu_all / gpu_s_all, "scenarios_per_hour": n_all / wall_all * 3600.0,
+            "serial_fp64_s": serial_meas_all,
+            "serial_fp64_measured": {str(k): {"scenarios": len(v), "seconds": v,
+                                              "of_class": len(by_side[k])} for k, v in measured.items()},
+            "serial_fp64_how": (f"{args.batch_fp64_per_class} whole scenarios per size class run alone through the "
+                                "FP64 plain path to their own end times; class mean x class count"),
+            "scenario_throughput_vs_serial_fp64": serial_meas_all / wall_all,
             "serial_fp64_plain_s_est": serial_all, "fp64_plain_rate_by_side": {str(k): v for k, v in rate64.items()},
-            "scenario_throughput_vs_serial_fp64": serial_all / wall_all,
             "horizon": "rain duration + 1800 s", "ranks": ws, "accuracy_vs_fp64": errors}
+
+
+def run_large(sw2d, dev, args, peak):
+    """The large-single-domain configuration: 8192 x 8192 cells of 2 m, the
+    catchment DEM with uniform n = 0.05, a Gaussian storm cell (80 mm/h,
+    sigma 2 km) moving at 10 m/s from the north-west corner along the
+    diagonal, open south edge, CFL 0.5.  Spun up in FP32 to t = 1800 s, then
+    `large_steps` windows of 48 iterations timed with CUDA events on the
+    solver's stream, L2 flushed between windows; the FP64 path then runs the
+    same simulated interval from the same state for the error of the FP32
+    result."""
+    import torch
+    from sw2d import large_domain as LD
+    from sw2d import scenarios as S
+    t0 = time.perf_counter()
+    s = S.catchment(LARGE, dx=LARGE_DX, seed=3, manning=0.05)
+    st = LD.storm_params(LARGE, LARGE_DX)
+
+    def solver(prec):
+        g = sw2d.Solver(rows=LARGE, cols=LARGE, dx=LARGE_DX, dy=LARGE_DX, precision=prec, dt_mode=sw2d.DT_CFL,
+                        dt=DT_MAX, cfl=0.5, south_open=1, manning=0.05, device=dev)
+        g.set_static(s["z"])
+        g.set_storm(st["peak"], st["x0"], st["y0"], st["vx"], st["vy"], st["sigma"])
+        return g
+
+    g = solver(sw2d.PREC_F32)
+    g.set_state(s["h0"])
+    g.advance(10 ** 9, t_end=LARGE_SPINUP_T)
+    t_start = g.budget()["t"]
+    strm = torch.cuda.ExternalStream(g.stream())
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")
+    g.advance(CHUNK)  # warm-up window (graph instantiation)
+    g.synchronize()
+    t_from = g.budget()["t"]
+    from_state = g.state()
+    times = []
+    for _ in range(args.large_steps):
+        with torch.cuda.stream(strm):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(strm)
+        n = g.advance(CHUNK)
+        e1.record(strm)
+        e1.synchronize()
+        assert n == CHUNK
+        times.append(e0.elapsed_time(e1) / 1e3)
+    bud = g.budget()
+    h32 = g.depth()
+    t_end = bud["t"]
+    kernel = g.describe()
+    g.close()
+    del flush
+    vol_err = abs(bud["volume"] - (bud["volume0"] + bud["rain_in"] + bud["source_in"] - bud["evap_out"] -
+                                   bud["outflow"] + bud["clamp_gain"])) / max(bud["volume"], 1e-30)
+    g64 = solver(sw2d.PREC_F64)
+    g64.set_state(from_state["h"], from_state["um"], from_state["vn"], t0=t_from)
+    n64 = g64.advance(10 ** 9, t_end=t_end)
+    h64 = g64.depth()
+    g64.close()
+    cells = LARGE * LARGE
+    per_launch = sum(times) / (CHUNK * len(times))
+    rate = cells / per_launch
+    err = depth_error(h64, h32)
+    err.update({"from_t_s": t_from, "to_t_s": t_end, "iterations_fp32": CHUNK * len(times),
+                "iterations_fp64": int(n64)})
+    return {"grid": [LARGE, LARGE], "dx": LARGE_DX, "cell_updates_per_s": rate, "launch_s": per_launch,
+            "windows": len(times), "iterations_per_window": CHUNK, "spinup_to_t_s": t_start,
+            "l2": "flushed between windows (256 MB write)", "kernel": kernel,
+            "roofline": {"bound": "hbm", "bytes_alg_per_cell_update": B_ALG_F32_SCALAR_N,
+                         "achieved": B_ALG_F32_SCALAR_N * rate / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": B_ALG_F32_SCALAR_N * rate / 1e9 / peak},
+            "volume_rel_error": vol_err, "wet_fraction": float(np.mean(h32 > 1.0e-4)),
+            "accuracy_vs_fp64": err, "wall_s": time.perf_counter() - t0}
+
+
+def fp64_alone(sw2d, dev, e):
+    """One scenario through the FP64 plain single-scenario path, alone, to its
+    end time: (seconds for set-up, run and depth download, depth, steps)."""
+    import torch
+    torch.cuda.synchronize()
+    tt = time.perf_counter()
+    g = sw2d.Solver(scen_cfg(sw2d, e["side"], precision=sw2d.PREC_F64, device=dev))
+    g.set_static(e["z"], e["n"])
+    g.set_state(e["h0"])
+    g.set_rain(sw2d.RAIN_LINEAR, e["rain"], e["rain_dt"])
+    g.advance(10 ** 9, t_end=e["t_end"])
+    h = g.depth()
+    steps = g.budget()["steps"]
+    sec = time.perf_counter() - tt
+    g.close()
+    return sec, h, steps
 
 
 def run_served(sw2d, dev, args):
@@ -439,12 +568,55 @@ def run_served(sw2d, dev, args):
                           depth=sp["h0"], manning=sp["n"], rain_kind=sw2d.RAIN_LINEAR, rain=sp["rain"],
                           rain_dt=sp["rain_dt"], t_end=sp["t_end"]) for k, sp in enumerate(specs)]
     budget = int(args.serve_gb * 2 ** 30)
-    srv = serve.Server(lambda: sw2d.Batch(device=dev, chunk=24, max_scenarios=len(reqs) + 8, max_bytes=budget),
+    # a sample of requests, spread over the sides up to 1024, whose served
+    # depth is kept for the comparison with the FP64 plain path
+    order = sorted((sp["side"], k) for k, sp in enumerate(specs) if sp["side"] <= 1024)
+    m = min(args.serve_fp64_sample, len(order))
+    sample = {order[int(round(i * (len(order) - 1) / max(m - 1, 1)))][1] for i in range(m)}
+    from sw2d import autotune
+    tick = autotune.apply_batch(sw2d.batch_config(device=dev)).chunk  # a tick is one graph replay
+    srv = serve.Server(lambda: sw2d.Batch(device=dev, max_scenarios=len(reqs) + 8, max_bytes=budget),
                        bytes_of=lambda r: sw2d.batch_scenario_bytes(r.cfg, 3, True), max_bytes=budget,
-                       launches_per_tick=24)
+                       launches_per_tick=tick, keep_results=lambda r: r.rid in sample)
     st = srv.run(reqs, timeout=600.0)
     srv.batch.close()
-    st.update({"rate_per_s": args.serve_rate, "memory_budget_gb": args.serve_gb})
+    st.update({"rate_per_s": args.serve_rate, "memory_budget_gb": args.serve_gb, "launches_per_tick": tick})
+    # the plain sequential FP64 path on the same request set: the sampled
+    # requests run alone in FP64 (measured: their time and their error); every
+    # other request's FP64 time is its served cell-updates at the FP64 rate
+    # measured on the sampled request nearest in side; then a one-at-a-time
+    # queue in arrival order gives the sequential path's time to result
+    served = {r.rid: r for r in srv.done if r.result and "steps" in r.result}
+    meas, errs = [], []
+    for k in sorted(sample):
+        if k not in served:
+            continue
+        sec, h64, steps = fp64_alone(sw2d, dev, specs[k])
+        side = specs[k]["side"]
+        meas.append({"side": side, "seconds": sec, "rate": side * side * steps / sec})
+        e = depth_error(h64, served[k].result["depth"])
+        e["side"] = side
+        errs.append(e)
+    if meas:
+        def fp64_seconds(r):
+            side = int(r.cfg.rows)
+            near = min(meas, key=lambda x: abs(np.log(x["side"] / side)))
+            return side * side * r.result["steps"] / near["rate"]
+        t_free, ttr = 0.0, []
+        for r in sorted(served.values(), key=lambda r: r.arrival):
+            t_free = max(t_free, r.arrival) + fp64_seconds(r)
+            ttr.append(t_free - r.arrival)
+        seq_s = sum(fp64_seconds(r) for r in served.values())
+        span = max(t_free, st["span_s"])
+        st["sequential_fp64"] = {
+            "how": (f"{len(meas)} requests (sides {min(x['side'] for x in meas)}-{max(x['side'] for x in meas)}) "
+                    "run alone through the FP64 plain path, measured; the others at the FP64 rate of the measured "
+                    "request nearest in side; a one-at-a-time queue in arrival order"),
+            "measured": meas, "busy_s": seq_s, "p50_s": float(np.percentile(ttr, 50)),
+            "p99_s": float(np.percentile(ttr, 99)), "scenarios_per_hour": len(served) / span * 3600.0,
+            "served_speedup_scenarios_per_hour": st["scenarios_per_hour"] / (len(served) / span * 3600.0)}
+        st["accuracy_vs_fp64"] = {"sample": errs, "max_abs_dh_m": max(e["max_abs_dh_m"] for e in errs),
+                                  "max_flooded_area_rel_diff": max(e["flooded_area_rel_diff"] for e in errs)}
     return st
 
 
@@ -508,11 +680,17 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--batched", type=int, default=1, help="run the batched-ensemble leg")
     ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--large", type=int, default=1, help="run the large-single-domain leg (8192^2, moving storm)")
+    ap.add_argument("--large-steps", type=int, default=3, help="timed 48-iteration windows of the large leg")
     ap.add_argument("--served", type=int, default=1, help="run the served-stream leg")
     ap.add_argument("--serve-rate", type=float, default=10.0)
     ap.add_argument("--serve-count", type=int, default=100)
     ap.add_argument("--serve-gb", type=float, default=40.0)
     ap.add_argument("--serve-sweep", default="", help="comma-separated arrival rates, e.g. 2,5,10,20,50")
+    ap.add_argument("--batch-fp64-per-class", type=int, default=4,
+                    help="whole scenarios per size class run through the FP64 plain path (serial baseline, accuracy)")
+    ap.add_argument("--serve-fp64-sample", type=int, default=6,
+                    help="served requests rerun alone through the FP64 plain path (sequential baseline, accuracy)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -51,7 +51,7 @@ class Request:
 
 class Server:
     def __init__(self, batch_factory: Callable[[], object], bytes_of: Callable[[Request], int],
-                 max_bytes: int, launches_per_tick: int = 24, keep_results: bool = False,
+                 max_bytes: int, launches_per_tick: int = 24, keep_results=False,
                  clock: Callable[[], float] = time.perf_counter, sleep: Callable[[float], None] = time.sleep):
         self.batch = batch_factory()
         # scenario slots of the batch (0 = no limit known): a request waits for
@@ -149,7 +149,8 @@ class Server:
             if sid in self.running and not st["running"]:
                 req = self.running.pop(sid)
                 res = {"t": st["t"], "steps": st["steps"], "budget": self.batch.budget(sid)}
-                if self.keep_results:
+                keep = self.keep_results(req) if callable(self.keep_results) else self.keep_results
+                if keep:  # True, or a predicate choosing the requests whose depth raster is kept
                     res["depth"] = self.batch.field(sid)
                 req.result = res
                 req.finished = self.now()
