@@ -354,6 +354,7 @@ def depth_error(a, b, th=1.0e-4):
     d = np.abs(a - b)
     wa, wb = int(np.count_nonzero(a > th)), int(np.count_nonzero(b > th))
     return {"max_abs_dh_m": float(d.max()), "p9999_abs_dh_m": float(np.percentile(d, 99.99)),
+            "cells_over_1mm": int(np.count_nonzero(d > 1e-3)), "cells": int(d.size),
             "flooded_area_rel_diff": abs(wa - wb) / max(wa, 1)}
 
 
@@ -418,17 +419,30 @@ def run_batched(sw2d, dev, args, rank=0, ws=1):
     by_side = {}
     for k, e in enumerate(ens):
         by_side.setdefault(e["side"], []).append(k)
+    # Beside the error of FP32, the conditioning of the same scenarios: the
+    # FP64 result's own change when the rain is raised by one part in a
+    # million (first two scenarios of each class).  Wet/dry thresholds and the
+    # dry-bed rules switch discontinuously, so over hours of simulated time
+    # the pointwise solution moves by millimetres under perturbations far
+    # below FP32 rounding.
     measured, errors = {}, []
     for side in sorted(by_side):
-        errs = []
-        for k in by_side[side][:args.batch_fp64_per_class]:
+        errs, sens = [], []
+        for n, k in enumerate(by_side[side][:args.batch_fp64_per_class]):
             sec, h64, _ = fp64_alone(sw2d, dev, ens[k])
             measured.setdefault(side, []).append(sec)
             errs.append(depth_error(h64, b.field(ids[k], sw2d.FIELD_DEPTH)))
+            if n < 2:
+                sens.append(depth_error(h64, fp64_alone(sw2d, dev, ens[k], rain_scale=1.0 + 1e-6)[1]))
         errors.append({"side": side, "scenarios": len(errs),
                        "max_abs_dh_m": max(x["max_abs_dh_m"] for x in errs),
                        "p9999_abs_dh_m": max(x["p9999_abs_dh_m"] for x in errs),
-                       "flooded_area_rel_diff": max(x["flooded_area_rel_diff"] for x in errs)})
+                       "cells_over_1mm": sum(x["cells_over_1mm"] for x in errs),
+                       "flooded_area_rel_diff": max(x["flooded_area_rel_diff"] for x in errs),
+                       "fp64_vs_fp64_rain_1e-6": {
+                           "scenarios": len(sens), "max_abs_dh_m": max(x["max_abs_dh_m"] for x in sens),
+                           "p9999_abs_dh_m": max(x["p9999_abs_dh_m"] for x in sens),
+                           "cells_over_1mm": sum(x["cells_over_1mm"] for x in sens)}})
     b.close()
     serial64_meas = sum(statistics.mean(measured[side]) * len(by_side[side]) for side in by_side)
     # the earlier estimate beside it: the FP64 rate on a 5 mm film per size
@@ -539,7 +553,7 @@ def run_large(sw2d, dev, args, peak):
             "accuracy_vs_fp64": err, "wall_s": time.perf_counter() - t0}
 
 
-def fp64_alone(sw2d, dev, e):
+def fp64_alone(sw2d, dev, e, rain_scale=1.0):
     """One scenario through the FP64 plain single-scenario path, alone, to its
     end time: (seconds for set-up, run and depth download, depth, steps)."""
     import torch
@@ -548,7 +562,7 @@ def fp64_alone(sw2d, dev, e):
     g = sw2d.Solver(scen_cfg(sw2d, e["side"], precision=sw2d.PREC_F64, device=dev))
     g.set_static(e["z"], e["n"])
     g.set_state(e["h0"])
-    g.set_rain(sw2d.RAIN_LINEAR, e["rain"], e["rain_dt"])
+    g.set_rain(sw2d.RAIN_LINEAR, np.asarray(e["rain"]) * rain_scale, e["rain_dt"])
     g.advance(10 ** 9, t_end=e["t_end"])
     h = g.depth()
     steps = g.budget()["steps"]
