@@ -97,17 +97,26 @@ cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_
     sh.pad = 0;
     // the general build carries the moving storm and the point sources
     const bool gen = F.rain_kind == RAIN_STORM || G.n_src > 0;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(nblocks);
+    lc.dynamicSmemBytes = 0;
+    lc.stream = st;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
 #define SW2D_L(id, nw, mb, un)                                                                             \
     if (variant == id) {                                                                                 \
+        lc.blockDim = dim3(nw * 32);                                                                     \
         if (S.rainw && gen)                                                                              \
-            stream_step_kernel<nw, mb, un, true, true><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh);   \
+            return cudaLaunchKernelEx(&lc, stream_step_kernel<nw, mb, un, true, true>, G, F, S, T, clk, ctl, slot, sh);   \
         else if (S.rainw)                                                                                \
-            stream_step_kernel<nw, mb, un, true, false><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh);  \
+            return cudaLaunchKernelEx(&lc, stream_step_kernel<nw, mb, un, true, false>, G, F, S, T, clk, ctl, slot, sh);  \
         else if (gen)                                                                                    \
-            stream_step_kernel<nw, mb, un, false, true><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh);  \
+            return cudaLaunchKernelEx(&lc, stream_step_kernel<nw, mb, un, false, true>, G, F, S, T, clk, ctl, slot, sh);  \
         else                                                                                             \
-            stream_step_kernel<nw, mb, un, false, false><<<nblocks, nw * 32, 0, st>>>(G, F, S, T, clk, ctl, slot, sh); \
-        return cudaGetLastError();                                                                       \
+            return cudaLaunchKernelEx(&lc, stream_step_kernel<nw, mb, un, false, false>, G, F, S, T, clk, ctl, slot, sh); \
     }
     SW2D_STREAM_VARIANTS(SW2D_L)
 #undef SW2D_L

@@ -19,13 +19,18 @@
 //                    forcing at t+dt, CFL bound of the owned faces
 //     so every quantity is computed once per cell and row, in registers;
 //   * west/east neighbours come from warp shuffles, except the neighbours'
-//     depths and discharges that each lane loads itself (they make the
-//     window's edge lanes exact); there is no shared-memory tile and no
-//     block-wide barrier inside the row loop;
+//     depths and y discharge that each lane loads itself (they make the
+//     window's edge lanes exact); an upwinded flux shared by two faces is
+//     formed once (the next row's, or the neighbour lane's, by a shuffle);
+//     there is no shared-memory tile and no block-wide barrier inside the
+//     row loop;
 //   * the next row's loads are issued before the current row's arithmetic.
 //
 // Budgets and the CFL bound are reduced per warp and then per CTA; the last
-// CTA of the launch finalises the clock slot (finish_cta_warp).
+// CTA of the launch finalises the clock slot (finish_cta_warp).  Launches
+// are programmatic dependents of the previous iteration (launch_stream_step):
+// the next grid's CTAs are scheduled while this one drains and finalises,
+// and wait for its completion before they read anything.
 #pragma once
 
 #include "sw2d_stream_unit.cuh"
@@ -46,6 +51,11 @@ __global__ void __launch_bounds__(NWARP * 32, MINB)
     stream_step_kernel(const GridDesc G, const ForcingDesc F, const StateBufs<float> S, const Thr<float> T,
                        Clock *__restrict__ clk, const Control *__restrict__ ctl, const int slot,
                        const StreamShape SH) {
+    // Launched as a programmatic dependent of the previous iteration: wait
+    // until that grid has completed and its writes are visible, then let the
+    // next iteration's grid be scheduled (its CTAs wait the same way)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int slot_out = slot == 2 ? 0 : slot + 1;
     const int slot_nx = slot == 0 ? 2 : slot - 1;

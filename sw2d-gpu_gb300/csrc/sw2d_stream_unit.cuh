@@ -19,13 +19,15 @@ namespace sw2d {
 // flags are exact from lane 1, the final depths from lane 2 (the west face
 // tests the west cell's flag) and the CFL bounds of the y-faces, which take
 // the west cell's final depth, from lane 3.  East: each lane loads its east
-// neighbour's depth and discharges and computes that lane's y-face velocity
-// itself, so the discharges of lane 31 are exact too; its provisional depth
-// is not (it needs lane 32's y-face discharge), so the dry-cell flags are
-// exact up to lane 30 and the final depths up to lane 29 (the east face
-// tests the east cell's flag).  Loading a neighbour's values in place of a
-// shuffle costs the same issue slot; recomputing lane -1's velocities as
-// well (a 2-lane west halo) cost more than the lane saved.
+// neighbour's depth and y discharge and computes that lane's y-face velocity
+// itself, so the y discharges of lane 31 are exact too; its x discharges are
+// not (the corner flux east of it is its east neighbour's, taken by a
+// shuffle) and neither is its provisional depth (it needs lane 32's y-face
+// discharge), so the dry-cell flags are exact up to lane 30 and the final
+// depths up to lane 29 (the east face tests the east cell's flag).  Loading
+// a neighbour's values in place of a shuffle costs the same issue slot;
+// recomputing lane -1's velocities as well (a 2-lane west halo) cost more
+// than the lane saved.
 constexpr int kStreamHL = 3;                            // west halo lanes
 constexpr int kStreamHR = 2;                            // east halo lanes
 constexpr int kStreamOut = 32 - kStreamHL - kStreamHR;  // output columns per warp
@@ -236,7 +238,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     // 29 columns past the east wall) all lie inside the zero frame around the
     // domain, whose zeros are the inactive-cell and wall values, so no load
     // needs a bounds test
-    float p_h, p_hw, p_hE, p_umE, p_vnE, p_dzx, p_dzy, p_n, p_um, p_vn, p_res;
+    float p_h, p_hw, p_hE, p_vnE, p_dzx, p_dzy, p_n, p_um, p_vn, p_res;
     unsigned p_m;
     int gp = (R0 - 4) * pitch + gj;  // element offset of the next row to read (fields fit 32-bit offsets)
     const int gp0 = gp;
@@ -251,7 +253,6 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         p_um = Uin[gp];
         p_vn = Vin[gp];
         p_hE = Hin[gp + 1];  // the east neighbour's depth and discharges
-        p_umE = Uin[gp + 1];
         p_vnE = Vin[gp + 1];
         gp += pitch;
     };
@@ -262,9 +263,11 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     float um1 = 0.f, um2 = 0.f, vn1 = 0.f, vn2 = 0.f;
     float uu_1 = 0.f, uu_2 = 0.f, uuL_1 = 0.f;
     float vv_1 = 0.f, vv_2 = 0.f, vvR_1 = 0.f, vvR_2 = 0.f;
-    float umE1 = 0.f, vnE1 = 0.f;  // the east neighbour's discharges of row r-1
+    float vnE1 = 0.f;  // the east neighbour's y discharge of row r-1
     float rum_2 = 0.f, rum_3 = 0.f, rvn_2 = 0.f, rvn_3 = 0.f;
     float hw_4 = 0.f;
+    float fx_1 = 0.f, cy_1 = 0.f;    // x flux through the cell north of the face, corner y flux (previous row)
+    float hmf_1 = 0.f, hnf_1 = 0.f;  // face depths of row r-1
     unsigned mb = 0u, mLb = 0u;  // bit k: active mask of row r-k (own / west column)
     unsigned db = 0u;            // bit k: row r-2-k is active and dry after the provisional update
 
@@ -274,7 +277,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     p_dzy = 0.f;
 #pragma unroll UNR
     for (int r = r_first; r < r_last; r++) {
-        const float hE0 = p_hE, umE0 = p_umE, vnE0 = p_vnE;
+        const float hE0 = p_hE, vnE0 = p_vnE;
         const float h0 = p_h, hL0 = p_hw, n0 = p_n, um0 = p_um, vn0 = p_vn;
         const float res3 = p_res;  // depth remainder of row r-3
         mb = (mb << 1) | p_m;
@@ -301,18 +304,31 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
 
         // ---- row r-1: new face discharges (cu:98-354) ----
         const int i = r - 1;
-        const float umE = umE1, umW = shup(um1);
-        const float vnE = vnE1, vnW = shup(vn1);
-        const float vvW = shup(vv_1);
+        const float umW = shup(um1);
+        const float vnE = vnE1;
+        // upwinded fluxes shared between neighbouring faces: the flux through
+        // the cell south of x-face i is the one north of face i+1 (kept for the
+        // next row); the corner flux east of a lane is the one west of its east
+        // neighbour (a shuffle); likewise along the rows for the y-faces
+        const float vx = uu_0 + uu_1;
+        const float fx_0 = vx * (vx >= 0.f ? um1 : um0);  // upw(uu_0 + uu_1, um0, um1)
+        const float vw2 = vv_1 + vv_2;
+        const float fw = vw2 * (vw2 >= 0.f ? umW : um1);  // upw_r(vv_1 + vv_2, umW, um1)
+        const float fe = shdn(fw);                        // the east lane's fw (lane 31: a halo lane)
+        const float vc = uu_0 + uuL_0;
+        const float cy_0 = vc * (vc >= 0.f ? vn1 : vn0);  // upw(uu_0 + uuL_0, vn0, vn1)
+        const float ve2 = vvR_1 + vv_1;
+        const float ge = ve2 * (ve2 >= 0.f ? vn1 : vnE);  // upw(vvR_1 + vv_1, vnE, vn1)
+        const float gw = shup(ge);                        // the west lane's ge (lane 0: a halo lane)
         float rum_1 = 0.f;
         {
             const float ha = h2, hb = h1, dz = dzx1;
             if (((mb >> 2) & (mb >> 1) & 1u) && ((ha >= gt_th) || (hb >= gt_th))) {
                 if (!dry_bed_dz(T, g, ha, hb, dz, rum_1)) {
-                    const float hm = 0.50f * (hb + ha);
+                    const float hm = hmf_1;  // 0.5 (hb + ha), formed with the velocities
                     const float u13 = g * hm * dt2dx * ((hb - ha) + dz);  // cu:166, hb + zb - ha - za
-                    const float u11 = hdx * (upw(uu_0 + uu_1, um0, um1) - upw_r(uu_1 + uu_2, um2, um1));
-                    const float u12c = hdy * (upw(vvR_1 + vvR_2, umE, um1) - upw_r(vv_1 + vv_2, umW, um1));
+                    const float u11 = hdx * (fx_0 - fx_1);
+                    const float u12c = hdy * (fe - fw);
                     const float u12 = not_col0 ? u12c : 0.f;  // zero on column 0 (cu:178-180)
                     const float vva = 0.250f * (vv_1 + vvR_1 + vv_2 + vvR_2);
                     const float ram = friction(0.5f * (n1 + n2), uu_1 * uu_1 + vva * vva, hm);
@@ -328,11 +344,11 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
             const float ha = hL1, hb = h1, dz = dzy1;
             if (((mLb >> 1) & (mb >> 1) & 1u) && ((ha >= gt_th) || (hb >= gt_th))) {
                 if (!dry_bed_dz(T, g, ha, hb, dz, rvn_1)) {
-                    const float hn = 0.50f * (hb + ha);
+                    const float hn = hnf_1;
                     const float v13 = g * hn * dt2dy * ((hb - ha) + dz);  // cu:283, hb + zb - ha - za
-                    const float v11c = hdx * (upw(uu_0 + uuL_0, vn0, vn1) - upw_r(uu_1 + uuL_1, vn2, vn1));
+                    const float v11c = hdx * (cy_0 - cy_1);
                     const float v11 = (i != 0) ? v11c : 0.f;  // zero on row 0 (cu:289-291)
-                    const float v12 = hdy * (upw(vvR_1 + vv_1, vnE, vn1) - upw_r(vv_1 + vvW, vnW, vn1));
+                    const float v12 = hdy * (ge - gw);
                     const float uua = 0.250f * (uu_1 + uu_0 + uuL_1 + uuL_0);
                     const float ram = friction(0.5f * (n1 + nL1), uua * uua + vv_1 * vv_1, hn);
                     rvn_1 = ((1.00f - dt2 * ram * 0.50f) * vn1 + (-v11 - v12 - v13)) /
@@ -436,9 +452,11 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         um2 = um1; um1 = um0; vn2 = vn1; vn1 = vn0;
         uu_2 = uu_1; uu_1 = uu_0; uuL_1 = uuL_0;
         vv_2 = vv_1; vv_1 = vv_0; vvR_2 = vvR_1; vvR_1 = vvE_0;
-        umE1 = umE0; vnE1 = vnE0;
+        vnE1 = vnE0;
         rum_3 = rum_2; rum_2 = rum_1; rvn_3 = rvn_2; rvn_2 = rvn_1;
         hw_4 = hw_3;
+        fx_1 = fx_0; cy_1 = cy_0;
+        hmf_1 = hmf; hnf_1 = hnf;
     }
 }
 
