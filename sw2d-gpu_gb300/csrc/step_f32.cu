@@ -5,6 +5,8 @@
 #include "sw2d_launch_impl.cuh"
 #include "sw2d_stream.cuh"
 
+#include <cstring>
+
 namespace sw2d {
 
 cudaError_t prepare_step(int th, int tw, float) {
@@ -38,9 +40,16 @@ constexpr int kStreamCarveoutPercent = 25;
 #define SW2D_STREAM_VARIANTS(X) \
     X(0, 2, 10, 2) X(1, 2, 10, 1) X(2, 4, 5, 2) X(3, 8, 2, 1) X(4, 8, 2, 2) X(5, 12, 2, 1)
 
-int stream_variants() { return 6; }
+// Build 6: the shape of build 0 with its rows staged in shared memory by TMA
+// (stream_step_tma_kernel), for uniform forcing; the other forcing forms run
+// build 0 (the same arithmetic, the same bits).
+constexpr int kTmaVariant = 6;
+constexpr size_t kTmaSmem = (size_t)2 * kTmaStages * kTmaStageBytes;
+
+int stream_variants() { return 7; }
 
 int stream_warps(int variant) {
+    if (variant == kTmaVariant) return 2;
 #define SW2D_W(id, nw, mb, un) \
     if (variant == id) return nw;
     SW2D_STREAM_VARIANTS(SW2D_W)
@@ -49,6 +58,16 @@ int stream_warps(int variant) {
 }
 
 cudaError_t prepare_stream_step(int variant) {
+    if (variant == kTmaVariant) {
+        cudaError_t e = cudaFuncSetAttribute(stream_step_tma_kernel<2, 10, 2>,
+                                             cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             (int)cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(stream_step_tma_kernel<2, 10, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kTmaSmem);
+        if (e != cudaSuccess) return e;
+        variant = 0;  // the build the other forcing forms run
+    }
 #define SW2D_P(id, nw, mb, un)                                                                            \
     if (variant == id) {                                                                               \
         const void *k[4] = {(const void *)stream_step_kernel<nw, mb, un, false, false>,                \
@@ -68,6 +87,7 @@ cudaError_t prepare_stream_step(int variant) {
 }
 
 const char *stream_variant_name(int variant) {
+    if (variant == kTmaVariant) return "stream_step_tma_kernel<2,10,2>";
 #define SW2D_N(id, nw, mb, un) \
     if (variant == id) return "stream_step_kernel<" #nw "," #mb "," #un ">";
     SW2D_STREAM_VARIANTS(SW2D_N)
@@ -77,6 +97,11 @@ const char *stream_variant_name(int variant) {
 
 int stream_ctas_per_sm(int variant) {
     int n = 0;
+    if (variant == kTmaVariant)
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stream_step_tma_kernel<2, 10, 2>, 64, kTmaSmem) ==
+                       cudaSuccess
+                   ? n
+                   : 0;
 #define SW2D_O(id, nw, mb, un)                                                                           \
     if (variant == id &&                                                                                 \
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stream_step_kernel<nw, mb, un, false, false>, nw * 32, 0) != \
@@ -86,6 +111,45 @@ int stream_ctas_per_sm(int variant) {
 #undef SW2D_O
     return n;
 }
+
+namespace {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry points (no link
+// against the driver library)
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+// Tensor map of one plane of the pitched layout, frame included, from its
+// cell-(0,0) pointer: dimensions (pitch, plane rows), boxes of one row.
+bool plane_map(CUtensorMap *m, const void *cell00, int rows, int pitch, bool u8) {
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn || !cell00) return false;
+    const size_t es = u8 ? 1 : 4;
+    char *base = (char *)cell00 - origin_for(pitch) * es;
+    cuuint64_t dims[2] = {(cuuint64_t)pitch, (cuuint64_t)(plane_for(rows, pitch) / pitch)};
+    cuuint64_t strides[1] = {(cuuint64_t)pitch * es};
+    cuuint32_t box[2] = {(cuuint32_t)(u8 ? kTmaBoxM : kTmaBoxF), 1u};
+    cuuint32_t estr[2] = {1u, 1u};
+    return fn(m, u8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box,
+              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
 
 cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_h, int units, const GridDesc &G,
                                const ForcingDesc &F, const StateBufs<float> &S, const Thr<float> &T, Clock *clk,
@@ -106,6 +170,26 @@ cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_
     lc.stream = st;
     lc.attrs = attr;
     lc.numAttrs = 1;
+    if (variant == kTmaVariant) {
+        if (!S.rainw && !gen) {
+            TmaMaps M;
+            std::memset(&M, 0, sizeof(M));
+            bool ok = true;
+            for (int b = 0; b < 2; b++)
+                ok = ok && plane_map(&M.h[b], S.h[b], G.rows, G.pitch, false) &&
+                     plane_map(&M.um[b], S.um[b], G.rows, G.pitch, false) &&
+                     plane_map(&M.vn[b], S.vn[b], G.rows, G.pitch, false) &&
+                     plane_map(&M.r[b], S.hr[b], G.rows, G.pitch, false);
+            ok = ok && plane_map(&M.dzx, S.dzx, G.rows, G.pitch, false) &&
+                 plane_map(&M.dzy, S.dzy, G.rows, G.pitch, false) && plane_map(&M.m, S.mask, G.rows, G.pitch, true);
+            if (S.nman) ok = ok && plane_map(&M.n, S.nman, G.rows, G.pitch, false);
+            if (!ok) return cudaErrorInvalidValue;
+            lc.blockDim = dim3(64);
+            lc.dynamicSmemBytes = kTmaSmem;
+            return cudaLaunchKernelEx(&lc, stream_step_tma_kernel<2, 10, 2>, G, F, S, T, clk, ctl, slot, sh, M);
+        }
+        variant = 0;
+    }
 #define SW2D_L(id, nw, mb, un)                                                                             \
     if (variant == id) {                                                                                 \
         lc.blockDim = dim3(nw * 32);                                                                     \

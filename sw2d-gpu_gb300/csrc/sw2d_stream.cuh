@@ -44,13 +44,15 @@ struct StreamShape {
     int pad;
 };
 
-// RAINW: per-cell rain factors; GEN: moving storm and point sources (the
-// launcher picks the build from the handle's forcing).
-template <int NWARP, int MINB, int UNR, bool RAINW, bool GEN>
-__global__ void __launch_bounds__(NWARP * 32, MINB)
-    stream_step_kernel(const GridDesc G, const ForcingDesc F, const StateBufs<float> S, const Thr<float> T,
-                       Clock *__restrict__ clk, const Control *__restrict__ ctl, const int slot,
-                       const StreamShape SH) {
+// The body of one launch.  RAINW: per-cell rain factors; GEN: moving storm
+// and point sources (the launcher picks the build from the handle's
+// forcing); TMA: rows staged in shared memory by TMA (M: the planes' tensor
+// maps, smem: kTmaStages stages per warp).
+template <int NWARP, int MINB, int UNR, bool RAINW, bool GEN, bool TMA>
+__device__ __forceinline__ void stream_step_body(const GridDesc &G, const ForcingDesc &F, const StateBufs<float> &S,
+                                                 const Thr<float> &T, Clock *__restrict__ clk,
+                                                 const Control *__restrict__ ctl, const int slot,
+                                                 const StreamShape &SH, const TmaMaps *M, unsigned char *smem) {
     // Launched as a programmatic dependent of the previous iteration: wait
     // until that grid has completed and its writes are visible, then let the
     // next iteration's grid be scheduled (its CTAs wait the same way)
@@ -77,6 +79,12 @@ __global__ void __launch_bounds__(NWARP * 32, MINB)
     // every quantity derived from them to be warp-uniform and keeps them in
     // uniform registers (measured 7-8 % faster than the plain expression)
     const int unit = __shfl_sync(0xffffffffu, (int)blockIdx.x * NWARP + wid, 0);
+    __shared__ __align__(8) unsigned long long s_bar[TMA ? NWARP : 1][kTmaStages];
+    if (TMA && lane == 0) {
+        for (int k = 0; k < kTmaStages; k++) mbar_init(&s_bar[wid][k], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (TMA) __syncwarp();
     if (unit < SH.units) {
         StreamView V;
         const int b = ci.buf;
@@ -109,8 +117,15 @@ __global__ void __launch_bounds__(NWARP * 32, MINB)
         V.t1 = ci.plan.t1;
         V.dx = G.dx;
         V.dy = G.dy;
-        stream_unit<UNR, RAINW, GEN>(V, unit % SH.tiles_w, unit / SH.tiles_w, SH.strip_h, lane, s_sr[wid], s_sc[wid],
-                             s_q0[wid], s_q1[wid], A);
+        stream_unit<UNR, RAINW, GEN, TMA>(V, unit % SH.tiles_w, unit / SH.tiles_w, SH.strip_h, lane, s_sr[wid],
+                                          s_sc[wid], s_q0[wid], s_q1[wid], A, M, b,
+                                          TMA ? smem + wid * kTmaStages * kTmaStageBytes : nullptr,
+                                          TMA ? s_bar[wid] : nullptr);
+    }
+    if (TMA) {  // every copy issued was waited for: the barriers can go
+        __syncwarp();
+        if (lane == 0)
+            for (int k = 0; k < kTmaStages; k++) mbar_inval(&s_bar[TMA ? wid : 0][k]);
     }
 
     // ---- warp, then CTA reductions; one thread accumulates and finishes ----
@@ -148,6 +163,26 @@ __global__ void __launch_bounds__(NWARP * 32, MINB)
         if (many) atomicOr(&clk[slot_out].status, (unsigned)ST_TOO_MANY_LOCAL_SOURCES);
     }
     finish_cta_warp(lane, ci, clk[slot_out], clk[slot_nx], ci.plan, *ctl, G, F);
+}
+
+template <int NWARP, int MINB, int UNR, bool RAINW, bool GEN>
+__global__ void __launch_bounds__(NWARP * 32, MINB)
+    stream_step_kernel(const GridDesc G, const ForcingDesc F, const StateBufs<float> S, const Thr<float> T,
+                       Clock *__restrict__ clk, const Control *__restrict__ ctl, const int slot,
+                       const StreamShape SH) {
+    stream_step_body<NWARP, MINB, UNR, RAINW, GEN, false>(G, F, S, T, clk, ctl, slot, SH, nullptr, nullptr);
+}
+
+// The build that stages rows in shared memory by TMA (uniform forcing only):
+// kept as a measured alternative; the row copies cost more issue slots than
+// the loads they replace in this per-warp pipeline.
+template <int NWARP, int MINB, int UNR>
+__global__ void __launch_bounds__(NWARP * 32, MINB)
+    stream_step_tma_kernel(const GridDesc G, const ForcingDesc F, const StateBufs<float> S, const Thr<float> T,
+                           Clock *__restrict__ clk, const Control *__restrict__ ctl, const int slot,
+                           const StreamShape SH, const __grid_constant__ TmaMaps M) {
+    extern __shared__ __align__(1024) unsigned char s_stage[];
+    stream_step_body<NWARP, MINB, UNR, false, false, true>(G, F, S, T, clk, ctl, slot, SH, &M, s_stage);
 }
 
 }  // namespace sw2d

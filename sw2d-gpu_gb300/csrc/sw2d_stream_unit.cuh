@@ -7,9 +7,58 @@
 // sw2d_stream.cuh for the layout of the pipeline and the halo).
 #pragma once
 
+#include <cuda.h>
+
 #include "sw2d_device.cuh"
 
 namespace sw2d {
+
+// ---- rows staged in shared memory by TMA (the stream_step_tma_kernel build) ----
+//
+// Tensor maps of the planes a launch reads (pitched layout, frame included);
+// the copies address cells by plane coordinates (column + 4, row + 4).
+struct TmaMaps {
+    CUtensorMap h[2], um[2], vn[2], r[2], dzx, dzy, n, m;
+};
+constexpr int kTmaStages = 4;                 // row stages per warp
+constexpr int kTmaSlot = 256;                 // bytes per field box in a stage (128-byte aligned)
+constexpr int kTmaStageBytes = 8 * kTmaSlot;  // h, um, vn, n, remainder, dzx, dzy, mask
+constexpr int kTmaBoxF = 40;                  // FP32 box width: the window, its neighbours, alignment slack
+constexpr int kTmaBoxM = 48;                  // mask box width in bytes
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_inval(unsigned long long *bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Waits for the phase of parity `ph` with a bounded number of polls; false
+// when it gave up (the caller reports an error instead of hanging).
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned ph) {
+    for (int it = 0; it < (1 << 22); it++) {
+        unsigned ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(ph)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// One row box of a plane into shared memory, completing on `bar`.
+__device__ __forceinline__ void tma_row(unsigned dst, const CUtensorMap *map, int x, int y, unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"((unsigned long long)map), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
 
 // Halo lanes: lanes whose results are incomplete because a neighbour they
 // need lies outside the window (the shuffles return a lane's own value at the
@@ -134,10 +183,15 @@ struct StreamAcc {
 // face (cu:380-381), used by the open south edge.  Two rules of the
 // reference stay explicit: no cross advection u12 on column 0 (cu:178-180)
 // and no v11 on row 0 (cu:289-291).
-template <int UNR, bool RAINW, bool GEN>
+//
+// TMA: the rows come from shared memory, copied there by TMA (maps M, buffer
+// parity buf, the warp's kTmaStages stages at stg and their barriers at
+// bars) instead of being loaded by every lane.
+template <int UNR, bool RAINW, bool GEN, bool TMA = false>
 __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, const int rs, const int strip_h,
                                             const int lane, int *s_sr, int *s_sc, float *s_q0, float *s_q1,
-                                            StreamAcc &A) {
+                                            StreamAcc &A, const TmaMaps *M = nullptr, int buf = 0,
+                                            unsigned char *stg = nullptr, unsigned long long *bars = nullptr) {
     const int rows = wuni(V.rows), cols = wuni(V.cols), pitch = wuni(V.pitch), south_open = wuni(V.south_open);
     const float dt2 = wuni(V.LS.dt2), dt2dx = wuni(V.LS.dt2dx), dt2dy = wuni(V.LS.dt2dy);
     const float u_ev0 = wuni(V.LS.ev0), u_ev1 = wuni(V.LS.ev1), u_rr0 = wuni(V.LS.rr0), u_rr1 = wuni(V.LS.rr1);
@@ -243,7 +297,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     int gp = (R0 - 4) * pitch + gj;  // element offset of the next row to read (fields fit 32-bit offsets)
     const int gp0 = gp;
     int lrow = R0 - 4;  // row of the next load
-    auto load_row = [&]() {
+    auto load_row_global = [&]() {
         p_h = Hin[gp];
         p_hw = Hin[gp - 1];  // the west neighbour's depth, exact on lane 0 too
         p_res = lrow >= 3 ? Rin[gp - 3 * pitch] : 0.f;  // remainder of row lrow-3, used with this row
@@ -255,6 +309,66 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         p_hE = Hin[gp + 1];  // the east neighbour's depth and discharges
         p_vnE = Vin[gp + 1];
         gp += pitch;
+    };
+
+    const int r_first = R0 - 4, r_last = R1 + 3;
+    // TMA build: each warp keeps rows in kTmaStages stages, copied
+    // kTmaStages - 1 rows ahead of the row read from them; the stage of row k
+    // holds h, um, vn, n and the mask of row k, the remainder of row k - 3 and
+    // the bed differences of row k - 1.  Box origins are rounded down to a
+    // 16-byte boundary (4 FP32 columns, 16 mask bytes); the plane coordinates
+    // (column + 4, row + 4) are >= 0 except the remainder rows above the
+    // frame, which the copy fills with zeros (as the register build's 0).
+    // Every operand of a copy is warp-uniform (broadcast from lane 0).
+    const int xf = TMA ? wuni((gj0 + 3) & ~3) : 0, xm = TMA ? wuni((gj0 + 4) & ~15) : 0;
+    const int of = gj + 4 - xf, om = gj + 4 - xm;  // this lane's index in the boxes
+    const unsigned stg_s = TMA ? (unsigned)wuni((int)smem_u32(stg)) : 0u;
+    const unsigned bars_s = TMA ? (unsigned)wuni((int)smem_u32(bars)) : 0u;
+    const int ub = TMA ? wuni(buf) : 0;
+    const unsigned tx = (unsigned)((raster ? 7 : 6) * kTmaBoxF * 4 + kTmaBoxM);
+    auto issue = [&](int k) {  // one lane: row k into its stage
+        const int s = (k - r_first) % kTmaStages;
+        const unsigned st = stg_s + s * kTmaStageBytes, bar = bars_s + s * 8;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(tx) : "memory");
+        const int y = k + 4;
+        tma_row(st + 0 * kTmaSlot, &M->h[ub], xf, y, bar);
+        tma_row(st + 1 * kTmaSlot, &M->um[ub], xf, y, bar);
+        tma_row(st + 2 * kTmaSlot, &M->vn[ub], xf, y, bar);
+        if (raster) tma_row(st + 3 * kTmaSlot, &M->n, xf, y, bar);
+        tma_row(st + 4 * kTmaSlot, &M->r[ub], xf, y - 3, bar);
+        tma_row(st + 5 * kTmaSlot, &M->dzx, xf, y - 1, bar);
+        tma_row(st + 6 * kTmaSlot, &M->dzy, xf, y - 1, bar);
+        tma_row(st + 7 * kTmaSlot, &M->m, xm, y, bar);
+    };
+    auto load_row_tma = [&]() {
+        const int k = lrow - r_first;
+        const unsigned char *st = stg + (k % kTmaStages) * kTmaStageBytes;
+        if (!mbar_wait(bars_s + (k % kTmaStages) * 8, (unsigned)((k / kTmaStages) & 1))) A.bad = true;
+        const float *fh = reinterpret_cast<const float *>(st);
+        p_h = fh[of];
+        p_hw = fh[of - 1];
+        p_hE = fh[of + 1];
+        p_um = reinterpret_cast<const float *>(st + kTmaSlot)[of];
+        const float *fv = reinterpret_cast<const float *>(st + 2 * kTmaSlot);
+        p_vn = fv[of];
+        p_vnE = fv[of + 1];
+        p_n = raster ? reinterpret_cast<const float *>(st + 3 * kTmaSlot)[of] : manning;
+        p_res = reinterpret_cast<const float *>(st + 4 * kTmaSlot)[of];
+        p_dzx = reinterpret_cast<const float *>(st + 5 * kTmaSlot)[of];
+        p_dzy = reinterpret_cast<const float *>(st + 6 * kTmaSlot)[of];
+        p_m = (unsigned)(st + 7 * kTmaSlot)[om];
+        lrow++;
+        // the stage read before this one is free once every lane is past it;
+        // the proxy fence orders those reads before the copy that refills it
+        __syncwarp();
+        if (lrow - 1 + kTmaStages - 1 < r_last && lane == 0) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(lrow - 1 + kTmaStages - 1);
+        }
+    };
+    auto load_row = [&]() {
+        if constexpr (TMA) load_row_tma();
+        else load_row_global();
     };
 
     // register rings: suffix = rows back from the row being read (r)
@@ -271,10 +385,15 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     unsigned mb = 0u, mLb = 0u;  // bit k: active mask of row r-k (own / west column)
     unsigned db = 0u;            // bit k: row r-2-k is active and dry after the provisional update
 
-    const int r_first = R0 - 4, r_last = R1 + 3;
+    if constexpr (TMA) {
+        if (lane == 0)
+            for (int k = r_first; k < r_first + kTmaStages - 1 && k < r_last; k++) issue(k);
+    }
     load_row();
-    p_dzx = 0.f;  // the bed differences of row r_first - 1 are not used
-    p_dzy = 0.f;
+    if constexpr (!TMA) {
+        p_dzx = 0.f;  // the bed differences of row r_first - 1 are not used
+        p_dzy = 0.f;
+    }
 #pragma unroll UNR
     for (int r = r_first; r < r_last; r++) {
         const float hE0 = p_hE, vnE0 = p_vnE;
@@ -283,13 +402,19 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
         mb = (mb << 1) | p_m;
         const unsigned mL0 = __shfl_up_sync(0xffffffffu, p_m, 1);
         mLb = (mLb << 1) | mL0;
-        const float dzx1 = p_dzx, dzy1 = p_dzy;  // bed differences of row r-1
+        float dzx1 = p_dzx, dzy1 = p_dzy;  // bed differences of row r-1
+        if constexpr (TMA) {  // row r's stage holds those of row r-1; row r_first - 1's are not used
+            dzx1 = r > r_first ? dzx1 : 0.f;
+            dzy1 = r > r_first ? dzy1 : 0.f;
+        }
         if (r + 1 < r_last) load_row();  // prefetch the next row
-        // the bed differences are used one row after they are read, so they
-        // are read one row late (row r, for the next iteration) instead of
-        // passing through a register ring
-        p_dzx = DZX[(r - r_first) * pitch + gp0];
-        p_dzy = DZY[(r - r_first) * pitch + gp0];
+        if constexpr (!TMA) {
+            // the bed differences are used one row after they are read, so
+            // they are read one row late (row r, for the next iteration)
+            // instead of passing through a register ring
+            p_dzx = DZX[(r - r_first) * pitch + gp0];
+            p_dzy = DZY[(r - r_first) * pitch + gp0];
+        }
 
         const float nL0 = raster ? shup(n0) : manning;
         // ---- row r: face velocities (cu:363-453) ----

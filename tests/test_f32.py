@@ -115,6 +115,32 @@ def test_stream_variants_agree(sw2d_mod, variant):
     assert b0["t"] == b1["t"]
 
 
+@pytest.mark.parametrize("raster", [True, False])
+def test_stream_tma_build_agrees(sw2d_mod, raster):
+    """The build that stages rows in shared memory by TMA (variant 6, uniform
+    forcing only) gives the same bits as variant 0: per-cell or scalar n,
+    NODATA holes, step rain with runoff fractions and evaporation, an open
+    south edge, CFL steps, over strips whose first rows read remainder rows
+    above the frame (TMA's zero fill) and a last, shorter strip."""
+    rows, cols = 150, 170
+    s, z = _catchment(seed=8, rows=rows, cols=cols)
+    out = []
+    for v in (0, 6):
+        g = _f32(sw2d_mod, rows, cols, 5.0, z, s["h0"], n=s["n"] if raster else None, kernel=2, strip_h=16,
+                 variant=v, south_open=1, dt_mode=1, dt=2.0, manning=0.04, INT=0.2, INF=0.1, LWL=0.01,
+                 EV_WL_min=0.002)
+        g.set_rain(sw2d_mod.RAIN_STEP, [120.0, 30.0], 300.0)
+        g.set_evaporation([2.0e-7], 3600.0)
+        assert ("tma" in g.describe()) == (v == 6)
+        g.advance(150)
+        out.append((g.depth(), g.state(), g.budget()))
+        g.close()
+    (d0, s0, b0), (d1, s1, b1) = out
+    assert np.array_equal(d0, d1)
+    assert np.array_equal(s0["um"], s1["um"]) and np.array_equal(s0["vn"], s1["vn"])
+    assert b0["t"] == b1["t"] and b0["volume"] == b1["volume"]
+
+
 @pytest.mark.parametrize("shape", [(1, 1), (1, 9), (9, 1), (17, 33), (33, 17), (3, 65), (40, 26), (5, 50), (7, 57),
                                    (6, 113)])
 def test_stream_ragged_grids_vs_oracle(oracle_mod, sw2d_mod, shape):
