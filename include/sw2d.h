@@ -96,7 +96,14 @@ typedef struct {
     int32_t strip_h;        /* rows per warp of the FP32 streaming kernel, 0 = auto */
     int32_t variant;        /* streaming-kernel build (occupancy / unrolling), 0 = default;
                                chosen by the autotuner */
-    int32_t reserved[1];
+    int32_t steps_per_launch; /* iterations per kernel launch of the FP32 streaming kernel
+                               under SW2D_DT_FIXED: K >= 2 runs K iterations per cooperative
+                               launch, each warp starting its next iteration as soon as the
+                               units around it have finished theirs (same state, bit for bit,
+                               as one launch per iteration); 1 = one launch per iteration;
+                               0 = the library's choice (48 where the decomposition fits one
+                               wave of resident warps, else 1).  At most 1024; values >= 2
+                               with SW2D_DT_CFL or another kernel are SW2D_ERR_INVALID_ARG. */
 } sw2d_config;
 
 typedef struct {
@@ -220,12 +227,15 @@ int sw2d_checkpoint_load(sw2d_handle *h, const void *buf, int64_t bytes);
 int sw2d_synchronize(sw2d_handle *h);
 int sw2d_get_stream(sw2d_handle *h, void **stream);
 
-/* Number of step-kernel launches issued since sw2d_set_state (including
- * launches that found the run already finished and did no work). */
+/* Number of kernel launches of the time loop issued since sw2d_set_state:
+ * one per iteration (including launches that found the run already finished
+ * and did no work), or, with several iterations per launch, two per launch
+ * (the plan kernel and the cooperative step kernel). */
 int sw2d_launch_count(sw2d_handle *h, int64_t *launches);
 
 /* One line naming the step kernel build and the decomposition the handle
- * runs, e.g. "stream_step_kernel<2,10,2> forcing=uniform strip_h=52 units=3040 ctas=1520"
+ * runs, e.g. "stream_step_kernel<2,10,2> forcing=uniform strip_h=52 units=3040
+ * ctas=1520 steps_per_launch=1"
  * (written NUL-terminated, truncated to `n` bytes).  No reference
  * counterpart: the reference's launch shape is fixed at cu:1222-1235. */
 int sw2d_describe(const sw2d_handle *h, char *buf, int32_t n);

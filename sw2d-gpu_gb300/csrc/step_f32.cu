@@ -3,9 +3,11 @@
 // the FP64 oracle with stated tolerances, not bit for bit.
 #define SW2D_REAL float
 #include "sw2d_launch_impl.cuh"
+#include "sw2d_pipe.cuh"
 #include "sw2d_stream.cuh"
 
 #include <cstring>
+#include <numeric>
 
 namespace sw2d {
 
@@ -26,6 +28,28 @@ cudaError_t launch_step(int th, int tw, int nblocks, const GridDesc &G, const Fo
 }
 
 int stream_out_cols() { return kStreamOut; }
+
+namespace {
+
+// The launch shape: strips of at most strip_h rows, split evenly; for the
+// pipelined launches the units go to warps in a scattered order (a
+// multiplier near 0.618 units, coprime with units).
+StreamShape stream_shape(int rows, int tiles_w, int strip_h, int units, bool scatter) {
+    StreamShape sh;
+    sh.tiles_w = tiles_w;
+    sh.strips = (rows + strip_h - 1) / strip_h;
+    sh.units = units;
+    sh.perm = 1;
+    if (scatter && units > 2) {
+        int p = (int)(units * 0.6180339887498949);
+        if (p < 1) p = 1;
+        while (std::gcd(p, units) != 1) p++;
+        sh.perm = p;
+    }
+    return sh;
+}
+
+}  // namespace
 
 // Shared-memory share of the L1/shared split for the streaming kernel, in
 // percent.  Each CTA needs only a few KB (source slots and the reduction, plus
@@ -74,8 +98,13 @@ cudaError_t prepare_stream_step(int variant) {
                             (const void *)stream_step_kernel<nw, mb, un, false, true>,                 \
                             (const void *)stream_step_kernel<nw, mb, un, true, false>,                 \
                             (const void *)stream_step_kernel<nw, mb, un, true, true>};                 \
-        for (const void *f : k) {                                                                      \
-            cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout,   \
+        const void *p[4] = {(const void *)stream_pipe_kernel<nw, mb, un, false, false>,                \
+                            (const void *)stream_pipe_kernel<nw, mb, un, false, true>,                 \
+                            (const void *)stream_pipe_kernel<nw, mb, un, true, false>,                 \
+                            (const void *)stream_pipe_kernel<nw, mb, un, true, true>};                 \
+        for (int i = 0; i < 8; i++) {                                                                  \
+            cudaError_t e = cudaFuncSetAttribute(i < 4 ? k[i] : p[i - 4],                              \
+                                                 cudaFuncAttributePreferredSharedMemoryCarveout,       \
                                                  kStreamCarveoutPercent);                             \
             if (e != cudaSuccess) return e;                                                            \
         }                                                                                              \
@@ -110,6 +139,67 @@ int stream_ctas_per_sm(int variant) {
     SW2D_STREAM_VARIANTS(SW2D_O)
 #undef SW2D_O
     return n;
+}
+
+// Resident CTAs per SM of the build's pipelined form (every form of a build
+// has the same register budget and shared memory).
+int stream_pipe_ctas_per_sm(int variant) {
+    if (variant == kTmaVariant) variant = 0;  // the TMA build has no pipelined form: build 0's
+    int n = 0;
+#define SW2D_PO(id, nw, mb, un)                                                                          \
+    if (variant == id &&                                                                                 \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stream_pipe_kernel<nw, mb, un, false, false>, nw * 32, 0) != \
+            cudaSuccess)                                                                                 \
+        n = 0;
+    SW2D_STREAM_VARIANTS(SW2D_PO)
+#undef SW2D_PO
+    return n;
+}
+
+int stream_pipe_max_iters() { return kPipeMaxIters; }
+int stream_pipe_min_strip() { return kPipeMinStrip; }
+
+// The plan kernel, then one cooperative launch of K iterations.
+cudaError_t launch_stream_pipe(int variant, int nblocks, int tiles_w, int strip_h, int units, const GridDesc &G,
+                               const ForcingDesc &F, const StateBufs<float> &S, const Thr<float> &T, Clock *clk,
+                               const Control *ctl, int slot, Plan *plans, unsigned *words, unsigned *flags, int K,
+                               cudaStream_t st) {
+    const int strips = (G.rows + strip_h - 1) / strip_h;  // the shortest strip has rows / strips rows
+    if (K < 1 || K > kPipeMaxIters || (strips > 1 && G.rows / strips < kPipeMinStrip)) return cudaErrorInvalidValue;
+    pipe_plan_kernel<<<1, ((K + 31) / 32) * 32, 0, st>>>(G, F, clk, ctl, slot, plans, words, flags, units, K);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const StreamShape sh = stream_shape(G.rows, tiles_w, strip_h, units, true);
+    PipeDesc P;
+    P.plans = plans;
+    P.words = words;
+    P.flags = flags;
+    const bool gen = F.rain_kind == RAIN_STORM || G.n_src > 0;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;  // every unit resident: the waits between units end
+    attr[0].val.cooperative = 1;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(nblocks);
+    lc.dynamicSmemBytes = 0;
+    lc.stream = st;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    if (variant == kTmaVariant) variant = 0;
+#define SW2D_PL(id, nw, mb, un)                                                                            \
+    if (variant == id) {                                                                                 \
+        lc.blockDim = dim3(nw * 32);                                                                     \
+        if (S.rainw && gen)                                                                              \
+            return cudaLaunchKernelEx(&lc, stream_pipe_kernel<nw, mb, un, true, true>, G, F, S, T, clk, ctl, slot, sh, P);   \
+        else if (S.rainw)                                                                                \
+            return cudaLaunchKernelEx(&lc, stream_pipe_kernel<nw, mb, un, true, false>, G, F, S, T, clk, ctl, slot, sh, P);  \
+        else if (gen)                                                                                    \
+            return cudaLaunchKernelEx(&lc, stream_pipe_kernel<nw, mb, un, false, true>, G, F, S, T, clk, ctl, slot, sh, P);  \
+        else                                                                                             \
+            return cudaLaunchKernelEx(&lc, stream_pipe_kernel<nw, mb, un, false, false>, G, F, S, T, clk, ctl, slot, sh, P); \
+    }
+    SW2D_STREAM_VARIANTS(SW2D_PL)
+#undef SW2D_PL
+    return cudaErrorInvalidValue;
 }
 
 namespace {
@@ -154,11 +244,7 @@ bool plane_map(CUtensorMap *m, const void *cell00, int rows, int pitch, bool u8)
 cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_h, int units, const GridDesc &G,
                                const ForcingDesc &F, const StateBufs<float> &S, const Thr<float> &T, Clock *clk,
                                const Control *ctl, int slot, cudaStream_t st) {
-    StreamShape sh;
-    sh.tiles_w = tiles_w;
-    sh.strip_h = strip_h;
-    sh.units = units;
-    sh.pad = 0;
+    const StreamShape sh = stream_shape(G.rows, tiles_w, strip_h, units, false);
     // the general build carries the moving storm and the point sources
     const bool gen = F.rain_kind == RAIN_STORM || G.n_src > 0;
     cudaLaunchAttribute attr[1];

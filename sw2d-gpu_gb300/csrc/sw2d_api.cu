@@ -60,7 +60,15 @@ struct sw2d_handle {
     ForcingDesc F{};
     GridDesc G{};
     bool have_static = false, have_state = false, has_nraster = false;
-    long long launches = 0;
+    long long launches = 0;  // clock-slot rotations (one per launch that finalises a slot)
+    long long kernels = 0;   // kernel launches of the time loop
+    // several iterations per launch (fixed time step, streaming kernel):
+    // iterations per launch (0 = one launch per iteration), the plan table,
+    // its run count and abort word, and the per-unit progress counters
+    int pipe_k = 0;
+    Plan *d_plans = nullptr;
+    unsigned *d_words = nullptr;
+    unsigned *d_flags = nullptr;
     Clock clock{};  // last clock read back
     double volume0 = 0.0;
     cudaGraphExec_t graph = nullptr;
@@ -161,6 +169,11 @@ int validate(const sw2d_config *c, std::string *why) {
         return *why = "the streaming kernel is FP32 only", 0;
     if (c->strip_h < 0) return *why = "strip_h must be >= 0", 0;
     if (c->variant < 0 || c->variant >= stream_variants()) return *why = "unknown kernel variant", 0;
+    if (c->steps_per_launch < 0 || c->steps_per_launch > stream_pipe_max_iters())
+        return *why = "steps_per_launch must be in 0..1024", 0;
+    if (c->steps_per_launch > 1 &&
+        (c->dt_mode != SW2D_DT_FIXED || c->precision != SW2D_PREC_F32 || c->kernel == SW2D_KERNEL_TILE))
+        return *why = "steps_per_launch > 1 needs the FP32 streaming kernel and SW2D_DT_FIXED", 0;
     return 1;
 }
 
@@ -253,6 +266,17 @@ int auto_strip(int rows, int tiles_w, int variant, int device) {
         const long long k = w * resident / tw;  // strips per column tile that fill w waves
         sh = (rows + k - 1) / k;
     }
+    return (int)(sh < 16 ? 16 : sh);
+}
+
+// Strip height of the pipelined launches: every unit must be resident at
+// once (one wave), so strips are the shortest that fit one wave, at least 16
+// rows.  0 when even one-row strips would not fit.
+int pipe_strip(int rows, int tiles_w, long long resident) {
+    const long long tw = tiles_w > 0 ? tiles_w : 1;
+    const long long per_tile = resident / tw;  // strips per column tile that one wave holds
+    if (per_tile < 1) return 0;
+    const long long sh = (rows + per_tile - 1) / per_tile;
     return (int)(sh < 16 ? 16 : sh);
 }
 
@@ -373,12 +397,35 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
     if (h->stream_kernel) {
         const int oc = stream_out_cols();
         h->stream_tiles_w = (cfg->cols + oc - 1) / oc;
+        const int nw = stream_warps(h->variant);
         int sh = cfg->strip_h;
+        // several iterations per launch under the fixed time step, when every
+        // unit fits one wave of resident warps (asked for: an error otherwise)
+        if (cfg->dt_mode == SW2D_DT_FIXED && cfg->steps_per_launch != 1) {
+            int sms = 0;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg->device);
+            const long long resident = (long long)sms * stream_pipe_ctas_per_sm(h->variant) * nw;
+            const int psh = sh > 0 ? sh : pipe_strip(cfg->rows, h->stream_tiles_w, resident);
+            const long long strips = psh > 0 ? (cfg->rows + psh - 1) / psh : 0;
+            const long long units = (long long)h->stream_tiles_w * strips;
+            // strips split the rows evenly: the shortest has rows / strips rows
+            const bool tall = strips == 1 || (strips > 1 && cfg->rows / strips >= stream_pipe_min_strip());
+            if (tall && units > 0 && units <= resident) {
+                h->pipe_k = cfg->steps_per_launch > 1 ? cfg->steps_per_launch : kChunk;
+                sh = psh;
+            } else if (cfg->steps_per_launch > 1) {
+                h->err = "steps_per_launch > 1: the units must fit one wave of resident warps, in strips of at least 8 rows";
+                return bail(SW2D_ERR_INVALID_ARG);
+            }
+        }
         if (sh <= 0) sh = auto_strip(cfg->rows, h->stream_tiles_w, h->variant, cfg->device);
         h->strip_h = sh;
         h->stream_units = h->stream_tiles_w * ((cfg->rows + sh - 1) / sh);
-        const int nw = stream_warps(h->variant);
         h->nblocks = (h->stream_units + nw - 1) / nw;
+        if (h->pipe_k > 0 && (cudaMalloc((void **)&h->d_plans, (size_t)h->pipe_k * sizeof(Plan)) != cudaSuccess ||
+                              cudaMalloc((void **)&h->d_words, 2 * sizeof(unsigned)) != cudaSuccess ||
+                              cudaMalloc((void **)&h->d_flags, 2 * (size_t)h->stream_units * sizeof(unsigned)) != cudaSuccess))
+            return bail(SW2D_ERR_OOM);
     }
     G.dt_mode = cfg->dt_mode;
     G.south_open = cfg->south_open ? 1 : 0;
@@ -432,6 +479,9 @@ int sw2d_destroy(sw2d_handle *h) {
     cudaFree(h->partial);
     cudaFree(h->d_clk);
     cudaFree(h->d_ctl);
+    cudaFree(h->d_plans);
+    cudaFree(h->d_words);
+    cudaFree(h->d_flags);
     for (DevBuf *b : {&h->rain, &h->ev, &h->src_cell, &h->src_q, &h->probe_cells, &h->probe_out}) cudaFree(b->p);
     if (h->h_clk) cudaFreeHost(h->h_clk);
     if (h->h_ctl) cudaFreeHost(h->h_ctl);
@@ -541,6 +591,7 @@ int sw2d_set_state(sw2d_handle *h, const double *depth, const double *um, const 
                           cols, pitch, h->G.south_open, make_thr<float>(h->cfg).ge_th, h->cfg.g,
                           &h->d_clk[0].cmax_bits, h->stream));
     h->launches = 0;
+    h->kernels = 0;
     h->have_state = true;
     int rc = read_clock(h);
     if (rc) return rc;
@@ -676,18 +727,29 @@ int sw2d_advance(sw2d_handle *h, int64_t max_steps, double t_end, int64_t *steps
         std::memcpy(&cmax, &h->clock.cmax_bits, sizeof(double));
         if (!decide_step(h->clock.t, cmax, h->clock.steps, ctl, h->G, &dtn)) break;
         const long long remaining = ctl.step_limit - h->clock.steps;
-        if (remaining >= kChunk) {
+        if (h->pipe_k > 0) {
+            // up to pipe_k iterations in one cooperative launch (the plan
+            // kernel stops it at step_limit and t_end)
+            CK(h, launch_stream_pipe(h->variant, h->nblocks, h->stream_tiles_w, h->strip_h, h->stream_units, h->G,
+                                     h->F, make_bufs<float>(h), make_thr<float>(h->cfg), h->d_clk, h->d_ctl,
+                                     (int)(h->launches % 3), h->d_plans, h->d_words, h->d_flags, h->pipe_k,
+                                     h->stream));
+            h->launches++;
+            h->kernels += 2;
+        } else if (remaining >= kChunk) {
             if (!h->graph_valid) {
                 int rc = capture_graph(h);
                 if (rc) return rc;
             }
             CK(h, cudaGraphLaunch(h->graph, h->stream));
             h->launches += kChunk;
+            h->kernels += kChunk;
         } else {
             const long long n = ((remaining + 2) / 3) * 3;
             for (long long m = 0; m < n; m++) {
                 CK(h, launch_one(h, (int)((h->launches) % 3)));
                 h->launches++;
+                h->kernels++;
             }
         }
         int rc = read_clock(h);
@@ -698,6 +760,8 @@ int sw2d_advance(sw2d_handle *h, int64_t max_steps, double t_end, int64_t *steps
         }
         if (h->clock.status & ST_TOO_MANY_LOCAL_SOURCES)
             return fail(h, SW2D_ERR_INVALID_ARG, "more than 64 point sources fall in one tile");
+        if (h->clock.status & ST_PIPE_TIMEOUT)
+            return fail(h, SW2D_ERR_TIMEOUT, "a pipelined launch gave up waiting for a neighbouring unit");
         if (!h->clock.ran) break;
     }
     if (steps_done) *steps_done = h->clock.steps - start;
@@ -897,6 +961,7 @@ int sw2d_checkpoint_load(sw2d_handle *h, const void *buf, int64_t bytes) {
     CK(h, cudaMemcpyAsync(h->d_clk, h->h_clk, sizeof(Clock), cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     h->launches = 0;
+    h->kernels = 0;
     h->clock = c;
     h->volume0 = hd.volume0;
     h->have_state = true;
@@ -917,7 +982,7 @@ int sw2d_get_stream(sw2d_handle *h, void **stream) {
 
 int sw2d_launch_count(sw2d_handle *h, int64_t *launches) {
     if (!h || !launches) return SW2D_ERR_INVALID_ARG;
-    *launches = h->launches;
+    *launches = h->kernels;
     return SW2D_OK;
 }
 
@@ -927,9 +992,14 @@ int sw2d_describe(const sw2d_handle *h, char *buf, int32_t n) {
         // the forcing build the launcher picks (step_f32.cu): storm and point
         // sources, per-cell rain factors, or neither
         const bool gen = h->F.rain_kind == RAIN_STORM || h->G.n_src > 0;
-        snprintf(buf, (size_t)n, "%s forcing=%s%s strip_h=%d units=%d ctas=%d", stream_variant_name(h->variant),
-                 gen ? "storm/sources" : "uniform", h->use_rainw ? "+rain_weights" : "", h->strip_h,
-                 h->stream_units, h->nblocks);
+        if (h->pipe_k > 0)
+            snprintf(buf, (size_t)n, "stream_pipe_kernel%s forcing=%s%s strip_h=%d units=%d ctas=%d steps_per_launch=%d",
+                     std::strchr(stream_variant_name(h->variant), '<'), gen ? "storm/sources" : "uniform",
+                     h->use_rainw ? "+rain_weights" : "", h->strip_h, h->stream_units, h->nblocks, h->pipe_k);
+        else
+            snprintf(buf, (size_t)n, "%s forcing=%s%s strip_h=%d units=%d ctas=%d steps_per_launch=1",
+                     stream_variant_name(h->variant), gen ? "storm/sources" : "uniform",
+                     h->use_rainw ? "+rain_weights" : "", h->strip_h, h->stream_units, h->nblocks);
     }
     else
         snprintf(buf, (size_t)n, "step_kernel<%s,%d,%d> ctas=%d", is_f64(h) ? "double" : "float", h->tile_h,

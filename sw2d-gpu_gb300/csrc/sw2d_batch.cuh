@@ -121,7 +121,9 @@ __global__ void __launch_bounds__(NWARP * 32, MINB) batch_step_kernel(const Batc
             const int ct = ue.y % S.tiles_w, rs = ue.y / S.tiles_w;
             // batched scenarios take neither a storm nor point sources nor rain
             // factors (sw2d_batch_add accepts none), so the uniform-forcing unit
-            stream_unit<UNR, false, false>(V, ct, rs, S.strip_h, lane, s_sr[wid], s_sc[wid], s_q0[wid], s_q1[wid], A);
+            const int r0 = rs * S.strip_h;
+            stream_unit<UNR, false, false>(V, ct, r0, min(r0 + S.strip_h, V.rows), lane, s_sr[wid], s_sc[wid],
+                                           s_q0[wid], s_q1[wid], A);
             warp_reduce_acc(A);
             if (lane == 0) {
                 const double area = S.G.dx * S.G.dy, scale = ci.plan.d.dt2 * area;

@@ -42,7 +42,10 @@ namespace sw2d {
 
 enum { B_RAIN = 0, B_SRC = 1, B_EV = 2, B_OUT = 3, B_CLAMP = 4, B_N = 5 };
 
-enum { ST_TOO_MANY_LOCAL_SOURCES = 1 };
+// device-side status bits (sticky in the clock slots): more point sources in
+// one warp window or tile than the kernel holds; a bounded wait of the
+// pipelined launches gave up
+enum { ST_TOO_MANY_LOCAL_SOURCES = 1, ST_PIPE_TIMEOUT = 2 };
 
 constexpr int kMaxLocalSources = 64;
 constexpr int kBuckets = 16;
@@ -185,6 +188,12 @@ __host__ __device__ inline bool decide_step(double t, double cmax, long long ste
 
 // ---------------------------------------------------------------------------
 // forcing (stream_flow cu:526-555, evaporation_load cu:589-601)
+//
+// The products and sums a compiler could fuse into one FMA are written with
+// the _rn intrinsics, which it never fuses: the FP32 translation units
+// compile with contraction on, and the plans they form (per launch, and in
+// the pipelined launches' tables) must round exactly as the FP64 path's and
+// the oracle's.
 // ---------------------------------------------------------------------------
 __device__ inline double compat_series(const double *v, int n, double dtv, double t) {
     if (n <= 0) return 0.0;
@@ -192,7 +201,7 @@ __device__ inline double compat_series(const double *v, int n, double dtv, doubl
     int it = (int)(t / dtv);
     int a = it < n ? it : n - 1;
     int b = it + 1 < n ? it + 1 : n - 1;
-    return v[a] + (v[b] - v[a]) / (dtv * (t - dtv * (it)));
+    return v[a] + (v[b] - v[a]) / (dtv * __dsub_rn(t, __dmul_rn(dtv, (double)it)));
 }
 
 __device__ inline double rain_uniform(const ForcingDesc &F, double t) {
@@ -211,7 +220,7 @@ __device__ inline double rain_uniform(const ForcingDesc &F, double t) {
         long long k = (long long)floor(s);
         if (k >= F.n_rain - 1) return 0.0;
         double w = s - (double)k;
-        return (F.rain[k] + w * (F.rain[k + 1] - F.rain[k])) / 3.6e6;
+        return __dadd_rn(F.rain[k], __dmul_rn(w, F.rain[k + 1] - F.rain[k])) / 3.6e6;
     }
     default:
         return 0.0;
@@ -233,60 +242,32 @@ __device__ inline double source_rate(const ForcingDesc &F, int n_src, int s, dou
         int b = it + 1 < F.n_qrec ? it + 1 : F.n_qrec - 1;
         double qa = F.src_q[(size_t)a * n_src + s];
         double qb = F.src_q[(size_t)b * n_src + s];
-        q = qa + (qb - qa) / (F.dtoq * (t - F.dtoq * (it)));
+        q = qa + (qb - qa) / (F.dtoq * __dsub_rn(t, __dmul_rn(F.dtoq, (double)it)));
     }
     return q / area;
 }
 
-// The plan of the launch that reads clock slot c under control ctl.  Called
-// by all 32 lanes of one converged warp; every lane returns the same plan.
-// FP64 arithmetic on this GPU has long latencies (a division takes several
-// hundred cycles) and the plan lies on the critical path between two
-// launches, so the pairs of independent evaluations -- the forcing at t0 and
-// at t1, dt2/dx and dt2/dy -- run as one instruction stream on lanes 0 and 1
-// instead of one after the other.  Each value is computed by the same
-// operations as a serial evaluation would use.
-__device__ inline Plan make_plan_warp(const int lane, double t, unsigned long long cmax_bits, long long steps,
-                                      const Control &ctl, const GridDesc &G, const ForcingDesc &F) {
-    Plan p;
-    p.run = 0;
-    p.storm_on0 = p.storm_on1 = 0;
-    p.pad = 0;
-    p.t0 = t;
-    p.t1 = t;
-    p.dt = 0.0;
-    LaunchScalars<double> &d = p.d;
-    d.dt2 = d.dt2dx = d.dt2dy = 0.0;
-    d.rr0 = d.rr1 = d.ev0 = d.ev1 = 0.0;
-    d.sx0 = d.sy0 = d.sx1 = d.sy1 = 0.0;
-    double dt = 0.0;
-    if (decide_step(t, __longlong_as_double((long long)cmax_bits), steps, ctl, G, &dt)) {  // warp-uniform
-        p.run = 1;
-        p.dt = dt;
-        p.t1 = t + dt;
-        d.dt2 = 2.00 * dt;
-        const bool second = (lane & 1) != 0;  // lane 1: t1 and the y step; lane 0: t0 and the x step
-        const double tl = second ? p.t1 : p.t0;
-        const double q = d.dt2 / (second ? G.dy : G.dx);
-        const double rr = rain_uniform(F, tl);
-        const double ev = evap_rate(F, tl);
-        const double sx = F.storm_x0 + F.storm_vx * tl;
-        const double sy = F.storm_y0 + F.storm_vy * tl;
-        d.dt2dx = __shfl_sync(0xffffffffu, q, 0);
-        d.dt2dy = __shfl_sync(0xffffffffu, q, 1);
-        d.rr0 = __shfl_sync(0xffffffffu, rr, 0);
-        d.rr1 = __shfl_sync(0xffffffffu, rr, 1);
-        d.ev0 = __shfl_sync(0xffffffffu, ev, 0);
-        d.ev1 = __shfl_sync(0xffffffffu, ev, 1);
-        if (F.rain_kind == RAIN_STORM) {
-            p.storm_on0 = p.t0 < F.storm_tstop;
-            p.storm_on1 = p.t1 < F.storm_tstop;
-            d.sx0 = __shfl_sync(0xffffffffu, sx, 0);
-            d.sy0 = __shfl_sync(0xffffffffu, sy, 0);
-            d.sx1 = __shfl_sync(0xffffffffu, sx, 1);
-            d.sy1 = __shfl_sync(0xffffffffu, sy, 1);
-        }
-    }
+// One of the two evaluations a plan needs at time tl: the step over the cell
+// size (dt2/dx for the x step, dt2/dy for the y step), the uniform rain and
+// evaporation rates and the storm centre.  Inlined into both plan makers
+// below, so that a plan is formed by the same operations either way.
+struct PlanHalf {
+    double q, rr, ev, sx, sy;
+};
+
+__device__ __forceinline__ PlanHalf plan_half(const GridDesc &G, const ForcingDesc &F, double dt2, double tl,
+                                              bool second) {
+    PlanHalf h;
+    h.q = dt2 / (second ? G.dy : G.dx);
+    h.rr = rain_uniform(F, tl);
+    h.ev = evap_rate(F, tl);
+    h.sx = __dadd_rn(F.storm_x0, __dmul_rn(F.storm_vx, tl));
+    h.sy = __dadd_rn(F.storm_y0, __dmul_rn(F.storm_vy, tl));
+    return h;
+}
+
+__device__ __forceinline__ void plan_round(Plan &p) {
+    const LaunchScalars<double> &d = p.d;
     LaunchScalars<float> &f = p.f;
     f.dt2 = (float)d.dt2;
     f.dt2dx = (float)d.dt2dx;
@@ -299,6 +280,91 @@ __device__ inline Plan make_plan_warp(const int lane, double t, unsigned long lo
     f.sy0 = (float)d.sy0;
     f.sx1 = (float)d.sx1;
     f.sy1 = (float)d.sy1;
+}
+
+__device__ __forceinline__ void plan_clear(Plan &p, double t) {
+    p.run = 0;
+    p.storm_on0 = p.storm_on1 = 0;
+    p.pad = 0;
+    p.t0 = t;
+    p.t1 = t;
+    p.dt = 0.0;
+    LaunchScalars<double> &d = p.d;
+    d.dt2 = d.dt2dx = d.dt2dy = 0.0;
+    d.rr0 = d.rr1 = d.ev0 = d.ev1 = 0.0;
+    d.sx0 = d.sy0 = d.sx1 = d.sy1 = 0.0;
+}
+
+// The plan of the launch that reads clock slot c under control ctl.  Called
+// by all 32 lanes of one converged warp; every lane returns the same plan.
+// FP64 arithmetic on this GPU has long latencies (a division takes several
+// hundred cycles) and the plan lies on the critical path between two
+// launches, so the pairs of independent evaluations -- the forcing at t0 and
+// at t1, dt2/dx and dt2/dy -- run as one instruction stream on lanes 0 and 1
+// instead of one after the other.  Each value is computed by the same
+// operations as a serial evaluation would use (make_plan_serial).
+__device__ inline Plan make_plan_warp(const int lane, double t, unsigned long long cmax_bits, long long steps,
+                                      const Control &ctl, const GridDesc &G, const ForcingDesc &F) {
+    Plan p;
+    plan_clear(p, t);
+    LaunchScalars<double> &d = p.d;
+    double dt = 0.0;
+    if (decide_step(t, __longlong_as_double((long long)cmax_bits), steps, ctl, G, &dt)) {  // warp-uniform
+        p.run = 1;
+        p.dt = dt;
+        p.t1 = t + dt;
+        d.dt2 = 2.00 * dt;
+        const bool second = (lane & 1) != 0;  // lane 1: t1 and the y step; lane 0: t0 and the x step
+        const PlanHalf h = plan_half(G, F, d.dt2, second ? p.t1 : p.t0, second);
+        d.dt2dx = __shfl_sync(0xffffffffu, h.q, 0);
+        d.dt2dy = __shfl_sync(0xffffffffu, h.q, 1);
+        d.rr0 = __shfl_sync(0xffffffffu, h.rr, 0);
+        d.rr1 = __shfl_sync(0xffffffffu, h.rr, 1);
+        d.ev0 = __shfl_sync(0xffffffffu, h.ev, 0);
+        d.ev1 = __shfl_sync(0xffffffffu, h.ev, 1);
+        if (F.rain_kind == RAIN_STORM) {
+            p.storm_on0 = p.t0 < F.storm_tstop;
+            p.storm_on1 = p.t1 < F.storm_tstop;
+            d.sx0 = __shfl_sync(0xffffffffu, h.sx, 0);
+            d.sy0 = __shfl_sync(0xffffffffu, h.sy, 0);
+            d.sx1 = __shfl_sync(0xffffffffu, h.sx, 1);
+            d.sy1 = __shfl_sync(0xffffffffu, h.sy, 1);
+        }
+    }
+    plan_round(p);
+    return p;
+}
+
+// The same plan from one thread (the pipelined launches' plan tables).
+__device__ inline Plan make_plan_serial(double t, unsigned long long cmax_bits, long long steps, const Control &ctl,
+                                        const GridDesc &G, const ForcingDesc &F) {
+    Plan p;
+    plan_clear(p, t);
+    LaunchScalars<double> &d = p.d;
+    double dt = 0.0;
+    if (decide_step(t, __longlong_as_double((long long)cmax_bits), steps, ctl, G, &dt)) {
+        p.run = 1;
+        p.dt = dt;
+        p.t1 = t + dt;
+        d.dt2 = 2.00 * dt;
+        const PlanHalf h0 = plan_half(G, F, d.dt2, p.t0, false);
+        const PlanHalf h1 = plan_half(G, F, d.dt2, p.t1, true);
+        d.dt2dx = h0.q;
+        d.dt2dy = h1.q;
+        d.rr0 = h0.rr;
+        d.rr1 = h1.rr;
+        d.ev0 = h0.ev;
+        d.ev1 = h1.ev;
+        if (F.rain_kind == RAIN_STORM) {
+            p.storm_on0 = p.t0 < F.storm_tstop;
+            p.storm_on1 = p.t1 < F.storm_tstop;
+            d.sx0 = h0.sx;
+            d.sy0 = h0.sy;
+            d.sx1 = h1.sx;
+            d.sy1 = h1.sy;
+        }
+    }
+    plan_round(p);
     return p;
 }
 
@@ -372,9 +438,12 @@ __device__ inline void accumulate_slot(Clock &co, int bucket, const double v[B_N
 // buckets, folds the budgets, advances time, plans the next launch, and
 // clears slot `cn` for the launch after.  Called by all 32 lanes of one
 // converged warp: lane b reads bucket b, and a shuffle tree (the same in
-// every lane) takes their maximum and sums; lane 0 writes the slot.
+// every lane) takes their maximum and sums; lane 0 writes the slot.  `pl` is
+// the plan of the launch's last iteration and `iters` the number of
+// iterations the launch ran (more than one for the pipelined launches).
 __device__ inline void finalize_slot_warp(const int lane, const Clock &ci, Clock &co, Clock &cn, const Plan &pl,
-                                          const Control &ctl, const GridDesc &G, const ForcingDesc &F) {
+                                          const Control &ctl, const GridDesc &G, const ForcingDesc &F,
+                                          const int iters = 1) {
     volatile Clock *cov = &co;
     unsigned long long cm = 0ull;
     double sum[B_N];
@@ -391,7 +460,7 @@ __device__ inline void finalize_slot_warp(const int lane, const Clock &ci, Clock
         for (int k = 0; k < B_N; k++) sum[k] += __shfl_xor_sync(0xffffffffu, sum[k], o);
     }
     const double t_new = (pl.t0 + pl.dt) + pl.dt;  // cu:1297, cu:1335
-    const long long steps_new = ci.steps + 1;
+    const long long steps_new = ci.steps + iters;
     const Plan np = make_plan_warp(lane, t_new, cm, steps_new, ctl, G, F);
     if (lane == 0) {
         for (int k = 0; k < B_N; k++) co.step[k] = sum[k];
@@ -400,7 +469,7 @@ __device__ inline void finalize_slot_warp(const int lane, const Clock &ci, Clock
         co.t = t_new;
         co.dt = pl.dt;
         co.steps = steps_new;
-        co.buf = 1 - ci.buf;
+        co.buf = ci.buf ^ (iters & 1);
         co.ran = 1;
         co.nonfinite = cov->nonfinite | ci.nonfinite;
         co.status = cov->status | ci.status;
@@ -413,7 +482,8 @@ __device__ inline void finalize_slot_warp(const int lane, const Clock &ci, Clock
 // accumulate_slot; the last CTA of the launch finalises the slot.  No CTA
 // waits.
 __device__ inline void finish_cta_warp(const int lane, const Clock &ci, Clock &co, Clock &cn, const Plan &pl,
-                                       const Control &ctl, const GridDesc &G, const ForcingDesc &F) {
+                                       const Control &ctl, const GridDesc &G, const ForcingDesc &F,
+                                       const int iters = 1) {
     unsigned int ticket = 0u;
     if (lane == 0) {
         __threadfence();
@@ -422,7 +492,7 @@ __device__ inline void finish_cta_warp(const int lane, const Clock &ci, Clock &c
     ticket = __shfl_sync(0xffffffffu, ticket, 0);
     if (ticket != gridDim.x * gridDim.y - 1) return;
     __threadfence();
-    finalize_slot_warp(lane, ci, co, cn, pl, ctl, G, F);
+    finalize_slot_warp(lane, ci, co, cn, pl, ctl, G, F, iters);
 }
 
 // ---------------------------------------------------------------------------

@@ -71,6 +71,18 @@ cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_
                                const ForcingDesc &F, const StateBufs<float> &S, const Thr<float> &T, Clock *clk,
                                const Control *ctl, int slot, cudaStream_t st);
 
+// The same kernel running several iterations per launch (fixed time step
+// only; sw2d_pipe.cuh): occupancy of its pipelined form, its limits, and the
+// plan kernel + cooperative launch of K iterations (plans: K entries, words:
+// 2, flags: two per unit).
+int stream_pipe_ctas_per_sm(int variant);
+int stream_pipe_max_iters();
+int stream_pipe_min_strip();
+cudaError_t launch_stream_pipe(int variant, int nblocks, int tiles_w, int strip_h, int units, const GridDesc &G,
+                               const ForcingDesc &F, const StateBufs<float> &S, const Thr<float> &T, Clock *clk,
+                               const Control *ctl, int slot, Plan *plans, unsigned *words, unsigned *flags, int K,
+                               cudaStream_t st);
+
 constexpr int kVolumeBlocks = 1024;
 constexpr int kVolumeThreads = 256;
 

@@ -39,10 +39,23 @@ namespace sw2d {
 
 struct StreamShape {
     int tiles_w;  // column tiles of kStreamOut columns
-    int strip_h;  // output rows per warp
-    int units;    // tiles_w * number of strips
-    int pad;
+    int strips;   // strips per column tile: the rows split as evenly as whole rows allow
+    int units;    // tiles_w * strips
+    int perm;     // warp w runs unit (w * perm) % units (perm coprime with units; 1 = in order)
 };
+
+// Rows [r0, r1) of strip rs when `rows` are split into `strips` strips whose
+// heights differ by at most one row (the first rows % strips are the longer).
+__device__ __forceinline__ void strip_rows(int rows, int strips, int rs, int &r0, int &r1) {
+    const int q = rows / strips, rem = rows - q * strips;
+    r0 = rs * q + min(rs, rem);
+    r1 = r0 + q + (rs < rem ? 1 : 0);
+}
+
+// The unit warp w runs.
+__device__ __forceinline__ int unit_of_warp(const StreamShape &SH, int w) {
+    return SH.perm == 1 ? w : (int)(((long long)w * SH.perm) % SH.units);
+}
 
 // The body of one launch.  RAINW: per-cell rain factors; GEN: moving storm
 // and point sources (the launcher picks the build from the handle's
@@ -78,7 +91,8 @@ __device__ __forceinline__ void stream_step_body(const GridDesc &G, const Forcin
     // broadcast from lane 0: the compiler then knows the unit, its rows and
     // every quantity derived from them to be warp-uniform and keeps them in
     // uniform registers (measured 7-8 % faster than the plain expression)
-    const int unit = __shfl_sync(0xffffffffu, (int)blockIdx.x * NWARP + wid, 0);
+    const int w_unit = __shfl_sync(0xffffffffu, (int)blockIdx.x * NWARP + wid, 0);
+    const int unit = __shfl_sync(0xffffffffu, w_unit < SH.units ? unit_of_warp(SH, w_unit) : w_unit, 0);
     __shared__ __align__(8) unsigned long long s_bar[TMA ? NWARP : 1][kTmaStages];
     if (TMA && lane == 0) {
         for (int k = 0; k < kTmaStages; k++) mbar_init(&s_bar[wid][k], 1);
@@ -117,7 +131,11 @@ __device__ __forceinline__ void stream_step_body(const GridDesc &G, const Forcin
         V.t1 = ci.plan.t1;
         V.dx = G.dx;
         V.dy = G.dy;
-        stream_unit<UNR, RAINW, GEN, TMA>(V, unit % SH.tiles_w, unit / SH.tiles_w, SH.strip_h, lane, s_sr[wid],
+        int r0, r1;
+        strip_rows(G.rows, SH.strips, unit / SH.tiles_w, r0, r1);
+        r0 = __shfl_sync(0xffffffffu, r0, 0);  // the strip's rows, warp-uniform (see above)
+        r1 = __shfl_sync(0xffffffffu, r1, 0);
+        stream_unit<UNR, RAINW, GEN, TMA>(V, unit % SH.tiles_w, r0, r1, lane, s_sr[wid],
                                           s_sc[wid], s_q0[wid], s_q1[wid], A, M, b,
                                           TMA ? smem + wid * kTmaStages * kTmaStageBytes : nullptr,
                                           TMA ? s_bar[wid] : nullptr);

@@ -165,7 +165,7 @@ struct StreamAcc {
     bool too_many_sources;
 };
 
-// Advances column tile `ct`, row strip `rs` (strip height strip_h) of the
+// Advances column tile `ct`, rows r0 .. r1-1 (a strip) of the
 // scenario in V.  s_sr/s_sc/s_q0/s_q1 are this warp's slots for local point
 // sources (kStreamMaxSrc each).  UNR is the unrolling of the row loop;
 // RAINW builds in the per-cell rain factors (V.Win) and GEN the moving storm
@@ -187,11 +187,20 @@ struct StreamAcc {
 // TMA: the rows come from shared memory, copied there by TMA (maps M, buffer
 // parity buf, the warp's kTmaStages stages at stg and their barriers at
 // bars) instead of being loaded by every lane.
-template <int UNR, bool RAINW, bool GEN, bool TMA = false>
-__device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, const int rs, const int strip_h,
+//
+// PIPE: the state is read past the L1 cache (ld.global.cg): in the pipelined
+// launches other SMs rewrite the state between this warp's iterations, so a
+// line this SM cached in an earlier iteration must not be read again.  Once
+// the strip's first three output rows are written (all that the strip
+// above reads of this iteration) and the rows above the strip have been
+// read (all of the strip above that this iteration reads), lane 0 publishes
+// top_val at *top_flag with a release store.
+template <int UNR, bool RAINW, bool GEN, bool TMA = false, bool PIPE = false>
+__device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, const int r0, const int r1,
                                             const int lane, int *s_sr, int *s_sc, float *s_q0, float *s_q1,
                                             StreamAcc &A, const TmaMaps *M = nullptr, int buf = 0,
-                                            unsigned char *stg = nullptr, unsigned long long *bars = nullptr) {
+                                            unsigned char *stg = nullptr, unsigned long long *bars = nullptr,
+                                            unsigned *top_flag = nullptr, unsigned top_val = 0u) {
     const int rows = wuni(V.rows), cols = wuni(V.cols), pitch = wuni(V.pitch), south_open = wuni(V.south_open);
     const float dt2 = wuni(V.LS.dt2), dt2dx = wuni(V.LS.dt2dx), dt2dy = wuni(V.LS.dt2dy);
     const float u_ev0 = wuni(V.LS.ev0), u_ev1 = wuni(V.LS.ev1), u_rr0 = wuni(V.LS.rr0), u_rr1 = wuni(V.LS.rr1);
@@ -236,8 +245,7 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
 
     const int gj0 = ct * kStreamOut - kStreamHL;
     const int gj = gj0 + lane;
-    const int R0 = rs * strip_h;
-    const int R1 = min(R0 + strip_h, rows);
+    const int R0 = r0, R1 = r1;
     const bool out_col = lane >= kStreamHL && lane < kStreamHL + kStreamOut && gj < cols;
     const bool not_col0 = gj != 0;
 
@@ -297,17 +305,21 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     int gp = (R0 - 4) * pitch + gj;  // element offset of the next row to read (fields fit 32-bit offsets)
     const int gp0 = gp;
     int lrow = R0 - 4;  // row of the next load
+    auto ld_state = [](const float *p) -> float {
+        if constexpr (PIPE) return __ldcg(p);
+        else return *p;
+    };
     auto load_row_global = [&]() {
-        p_h = Hin[gp];
-        p_hw = Hin[gp - 1];  // the west neighbour's depth, exact on lane 0 too
-        p_res = lrow >= 3 ? Rin[gp - 3 * pitch] : 0.f;  // remainder of row lrow-3, used with this row
+        p_h = ld_state(Hin + gp);
+        p_hw = ld_state(Hin + gp - 1);  // the west neighbour's depth, exact on lane 0 too
+        p_res = lrow >= 3 ? ld_state(Rin + gp - 3 * pitch) : 0.f;  // remainder of row lrow-3, used with this row
         lrow++;
         p_n = raster ? Nin[gp] : manning;
         p_m = (unsigned)Min[gp];
-        p_um = Uin[gp];
-        p_vn = Vin[gp];
-        p_hE = Hin[gp + 1];  // the east neighbour's depth and discharges
-        p_vnE = Vin[gp + 1];
+        p_um = ld_state(Uin + gp);
+        p_vn = ld_state(Vin + gp);
+        p_hE = ld_state(Hin + gp + 1);  // the east neighbour's depth and discharges
+        p_vnE = ld_state(Vin + gp + 1);
         gp += pitch;
     };
 
@@ -569,6 +581,14 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
                 }
             }
             if (!isfinite(hw_3 + un + vw)) A.bad = true;  // a NaN or an infinity in any of the three
+        }
+
+        if constexpr (PIPE) {
+            if (r == R0 + 5) {  // output rows R0 .. R0+2 written; every row above R0 read
+                __syncwarp();
+                if (lane == 0)
+                    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(top_flag), "r"(top_val) : "memory");
+            }
         }
 
         // ---- advance the rings ----

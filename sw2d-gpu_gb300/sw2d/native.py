@@ -34,7 +34,7 @@ class Config(C.Structure):
         ("south_open", C.c_int32), ("device", C.c_int32),
         ("tile_h", C.c_int32), ("tile_w", C.c_int32),
         ("kernel", C.c_int32), ("strip_h", C.c_int32),
-        ("variant", C.c_int32), ("reserved", C.c_int32 * 1),
+        ("variant", C.c_int32), ("steps_per_launch", C.c_int32),
     ]
 
 
