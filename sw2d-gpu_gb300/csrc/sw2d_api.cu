@@ -188,6 +188,13 @@ void grid_shape(const sw2d_config *c, int *pitch, size_t *plane, int *th, int *t
 
 int read_clock(sw2d_handle *h) {
     const int slot = (int)(h->launches % 3);
+    // the streaming kernel leaves the budget fold of the slot its last
+    // launch wrote to the next launch (finish_cta_deferred_warp): fold it
+    // here (a fold is idempotent)
+    if (h->stream_kernel && h->pipe_k == 0 && h->have_state) {
+        fold_kernel<<<1, 32, 0, h->stream>>>(h->d_clk, slot, (slot + 2) % 3);
+        CK(h, cudaGetLastError());
+    }
     CK(h, cudaMemcpyAsync(h->h_clk, h->d_clk + slot, sizeof(Clock), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     h->clock = *h->h_clk;

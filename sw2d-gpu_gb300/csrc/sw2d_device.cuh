@@ -84,7 +84,7 @@ struct __align__(16) Clock {
     double tot_s[B_N], tot_c[B_N]; // Kahan running totals of the budgets [m^3]
     double step[B_N];              // budget sums of the iteration that wrote this slot
     unsigned int done_blocks;      // CTAs of the writing launch that have finished
-    unsigned int pad;
+    unsigned int fold_pending;     // step and totals not yet folded (finalize_slot_deferred_warp)
     Plan plan;                     // what the launch reading this slot does
     // accumulators of the writing launch, spread over kBuckets addresses so
     // that thousands of CTAs do not serialise on one atomic location; summed
@@ -493,6 +493,124 @@ __device__ inline void finish_cta_warp(const int lane, const Clock &ci, Clock &c
     if (ticket != gridDim.x * gridDim.y - 1) return;
     __threadfence();
     finalize_slot_warp(lane, ci, co, cn, pl, ctl, G, F, iters);
+}
+
+// ---- the same bookkeeping with the budget fold off the critical path ----
+//
+// The last CTA of a launch lies on the critical path between two launches;
+// of the slot it finalises, the next launch needs only the time, the step
+// count, the buffer and the plan (from the CFL bound).  The budget sums --
+// five FP64 shuffle trees and the Kahan fold, several microseconds of
+// FP64 latency on one warp -- are left in the slot's buckets and folded by
+// the FIRST CTA to finish the next launch (fold_slot_warp), tens of
+// microseconds before that launch ends, or by fold_kernel after the host's
+// last launch.  A fold reads the slot's buckets and the previous slot's
+// step and totals, all final by then, and writes only the slot's own step
+// and totals; the slot's fold_pending flag makes it happen once (a slot
+// set by the host -- a new state, a restored checkpoint -- has nothing to
+// fold), and the accumulators a launch clears for the launch after leave
+// step and totals alone.
+
+// Folds slot c, written by the launch that read slot prev: c.step = its
+// bucket sums (the shuffle tree of finalize_slot_warp), c.tot = prev.tot +
+// prev.step (Kahan).  All 32 lanes of one converged warp.
+__device__ inline void fold_slot_warp(const int lane, const Clock &prev, Clock &c) {
+    volatile Clock *cv = &c;
+    if (cv->fold_pending == 0u) return;  // the same value in every lane
+    double sum[B_N];
+    for (int k = 0; k < B_N; k++) sum[k] = lane < kBuckets ? cv->stepb[k][lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < B_N; k++) sum[k] += __shfl_xor_sync(0xffffffffu, sum[k], o);
+    }
+    if (lane == 0) {
+        for (int k = 0; k < B_N; k++) c.step[k] = sum[k];
+        fold_totals(prev, c);
+        c.fold_pending = 0u;
+    }
+}
+
+// clear_slot_accumulators_warp without the step sums (see above).
+__device__ inline void clear_slot_buckets_warp(const int lane, Clock &c) {
+    if (lane < kBuckets) {
+        c.cmaxb[lane] = 0ull;
+        for (int k = 0; k < B_N; k++) c.stepb[k][lane] = 0.0;
+    }
+    if (lane == 0) {
+        c.cmax_bits = 0ull;
+        c.nonfinite = 0u;
+        c.status = 0u;
+        c.done_blocks = 0u;
+    }
+}
+
+// finalize_slot_warp for one iteration without the budgets: the CFL bound
+// (an integer maximum of the buckets' bits), time, plan, flags.
+__device__ inline void finalize_slot_deferred_warp(const int lane, const Clock &ci, Clock &co, Clock &cn,
+                                                   const Plan &pl, const Control &ctl, const GridDesc &G,
+                                                   const ForcingDesc &F) {
+    volatile Clock *cov = &co;
+    unsigned long long cm = lane < kBuckets ? cov->cmaxb[lane] : 0ull;
+    unsigned int nf = lane == 16 ? cov->nonfinite : 0u;
+    unsigned int st = lane == 17 ? cov->status : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long c2 = __shfl_xor_sync(0xffffffffu, cm, o);
+        cm = c2 > cm ? c2 : cm;
+    }
+    nf = __shfl_sync(0xffffffffu, nf, 16);
+    st = __shfl_sync(0xffffffffu, st, 17);
+    const double t_new = (pl.t0 + pl.dt) + pl.dt;  // cu:1297, cu:1335
+    const long long steps_new = ci.steps + 1;
+    const Plan np = make_plan_warp(lane, t_new, cm, steps_new, ctl, G, F);
+    if (lane == 0) {
+        co.cmax_bits = cm;
+        co.t = t_new;
+        co.dt = pl.dt;
+        co.steps = steps_new;
+        co.buf = 1 - ci.buf;
+        co.ran = 1;
+        co.nonfinite = nf | ci.nonfinite;
+        co.status = st | ci.status;
+        co.plan = np;
+        co.fold_pending = 1u;
+    }
+    clear_slot_buckets_warp(lane, cn);
+}
+
+// finish_cta_warp with the deferred fold: the first CTA to finish folds the
+// slot this launch read (written by the previous launch), the last
+// finalises the slot this launch wrote.  clk, and the three slot indices as
+// in the step kernels.
+__device__ inline void finish_cta_deferred_warp(const int lane, Clock *clk, const int slot, const int slot_out,
+                                                const int slot_nx, const Plan &pl, const Control &ctl,
+                                                const GridDesc &G, const ForcingDesc &F) {
+    unsigned int ticket = 0u;
+    if (lane == 0) {
+        __threadfence();
+        ticket = atomicAdd(&clk[slot_out].done_blocks, 1u);
+    }
+    ticket = __shfl_sync(0xffffffffu, ticket, 0);
+    const unsigned int last = gridDim.x * gridDim.y - 1;
+    if (ticket == 0u) fold_slot_warp(lane, clk[slot_nx], clk[slot]);
+    if (ticket != last) return;
+    __threadfence();
+    finalize_slot_deferred_warp(lane, clk[slot], clk[slot_out], clk[slot_nx], pl, ctl, G, F);
+}
+
+// A launch whose plan says "do not run", with the deferred fold: one warp
+// folds the slot it read, then carries it (carry_slot).
+__device__ inline void carry_slot_deferred_warp(const int lane, Clock *clk, const int slot, const int slot_out,
+                                                const int slot_nx) {
+    fold_slot_warp(lane, clk[slot_nx], clk[slot]);
+    __syncwarp();
+    if (lane == 0) carry_slot(clk[slot], clk[slot_out], clk[slot_nx]);
+}
+
+// Folds slot `slot` (see above) after the last launch the host issued.
+static __global__ void fold_kernel(Clock *__restrict__ clk, const int slot, const int prev) {
+    fold_slot_warp((int)threadIdx.x, clk[prev], clk[slot]);
 }
 
 // ---------------------------------------------------------------------------

@@ -27,7 +27,9 @@
 //   * the next row's loads are issued before the current row's arithmetic.
 //
 // Budgets and the CFL bound are reduced per warp and then per CTA; the last
-// CTA of the launch finalises the clock slot (finish_cta_warp).  Launches
+// CTA of the launch finalises the clock slot's time and plan, the first to
+// finish folds the budgets of the slot the launch read
+// (finish_cta_deferred_warp).  Launches
 // are programmatic dependents of the previous iteration (launch_stream_step):
 // the next grid's CTAs are scheduled while this one drains and finalises,
 // and wait for its completion before they read anything.
@@ -76,7 +78,7 @@ __device__ __forceinline__ void stream_step_body(const GridDesc &G, const Forcin
     const int slot_nx = slot == 0 ? 2 : slot - 1;
     const Clock &ci = clk[slot];
     if (!ci.plan.run) {
-        if (blockIdx.x == 0 && tid == 0) carry_slot(ci, clk[slot_out], clk[slot_nx]);
+        if (blockIdx.x == 0 && wid == 0) carry_slot_deferred_warp(lane, clk, slot, slot_out, slot_nx);
         return;
     }
 
@@ -180,7 +182,7 @@ __device__ __forceinline__ void stream_step_body(const GridDesc &G, const Forcin
         accumulate_slot(clk[slot_out], blockIdx.x % kBuckets, v, (double)cmb, anybad);
         if (many) atomicOr(&clk[slot_out].status, (unsigned)ST_TOO_MANY_LOCAL_SOURCES);
     }
-    finish_cta_warp(lane, ci, clk[slot_out], clk[slot_nx], ci.plan, *ctl, G, F);
+    finish_cta_deferred_warp(lane, clk, slot, slot_out, slot_nx, ci.plan, *ctl, G, F);
 }
 
 template <int NWARP, int MINB, int UNR, bool RAINW, bool GEN>
