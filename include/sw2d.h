@@ -101,9 +101,10 @@ typedef struct {
                                launch, each warp starting its next iteration as soon as the
                                units around it have finished theirs (same state, bit for bit,
                                as one launch per iteration); 1 = one launch per iteration;
-                               0 = the library's choice (48 where the decomposition fits one
-                               wave of resident warps, else 1).  At most 1024; values >= 2
-                               with SW2D_DT_CFL or another kernel are SW2D_ERR_INVALID_ARG. */
+                               0 = the library's choice (48 where one wave of resident warps
+                               holds the grid in strips of at most 32 rows -- grids up to
+                               about 1600^2 --, else 1).  At most 1024; values >= 2 with
+                               SW2D_DT_CFL or another kernel are SW2D_ERR_INVALID_ARG. */
 } sw2d_config;
 
 typedef struct {
@@ -230,7 +231,9 @@ int sw2d_get_stream(sw2d_handle *h, void **stream);
 /* Number of kernel launches of the time loop issued since sw2d_set_state:
  * one per iteration (including launches that found the run already finished
  * and did no work), or, with several iterations per launch, two per launch
- * (the plan kernel and the cooperative step kernel). */
+ * (the plan kernel and the cooperative step kernel); plus, per advance, the
+ * kernel that plans its first launch and, for the streaming kernel with one
+ * launch per iteration, the one that folds the last launch's budgets. */
 int sw2d_launch_count(sw2d_handle *h, int64_t *launches);
 
 /* One line naming the step kernel build and the decomposition the handle

@@ -194,6 +194,7 @@ int read_clock(sw2d_handle *h) {
     if (h->stream_kernel && h->pipe_k == 0 && h->have_state) {
         fold_kernel<<<1, 32, 0, h->stream>>>(h->d_clk, slot, (slot + 2) % 3);
         CK(h, cudaGetLastError());
+        h->kernels++;
     }
     CK(h, cudaMemcpyAsync(h->h_clk, h->d_clk + slot, sizeof(Clock), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
@@ -260,6 +261,10 @@ int upload_table(sw2d_handle *h, DevBuf &b, const T *src, size_t n) {
 // (longer strips measured slower on GB300 at 4096^2 and up), and at least 16
 // rows, since each strip recomputes 7 halo rows.
 constexpr long long kMaxAutoStrip = 160;
+
+// Longest one-wave strip for which the library picks several iterations per
+// launch by itself (steps_per_launch = 0).
+constexpr int kAutoPipeMaxStrip = 32;
 
 int auto_strip(int rows, int tiles_w, int variant, int device) {
     int sms = 0;
@@ -417,7 +422,13 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
             const long long units = (long long)h->stream_tiles_w * strips;
             // strips split the rows evenly: the shortest has rows / strips rows
             const bool tall = strips == 1 || (strips > 1 && cfg->rows / strips >= stream_pipe_min_strip());
-            if (tall && units > 0 && units <= resident) {
+            // the library's choice: pipelined where one wave holds the grid in
+            // short strips (measured on GB300: 1.12-1.30x faster than one launch
+            // per iteration up to 1024^2, whose iterations are mostly the
+            // grid-wide drain; about even with 52-row strips at 2048^2, slower
+            // with the long strips one wave needs beyond)
+            const bool worth = cfg->steps_per_launch > 1 || psh <= kAutoPipeMaxStrip;
+            if (tall && worth && units > 0 && units <= resident) {
                 h->pipe_k = cfg->steps_per_launch > 1 ? cfg->steps_per_launch : kChunk;
                 sh = psh;
             } else if (cfg->steps_per_launch > 1) {
@@ -728,6 +739,7 @@ int sw2d_advance(sw2d_handle *h, int64_t max_steps, double t_end, int64_t *steps
     // plan the next launch under the new control and the current forcing
     plan_kernel<<<1, 32, 0, h->stream>>>(h->G, h->F, h->d_clk, h->d_ctl, (int)(h->launches % 3));
     CK(h, cudaGetLastError());
+    h->kernels++;
     for (;;) {
         double dtn;
         double cmax;

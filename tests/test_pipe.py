@@ -73,8 +73,8 @@ def test_pipe_uniform_forcing_matches_one_launch_per_iteration(sw2d_mod, spl):
         assert _run(g, (150, 37)) == 187
         out.append(g)
     _same(*out)
-    # the pipelined handle issues two kernels per launch
-    assert out[1].launch_count() == 2 * sum(-(-c // (48 if spl == 0 else spl)) for c in (150, 37))
+    # the pipelined handle issues two kernels per launch, and one plan kernel per advance
+    assert out[1].launch_count() == 2 * sum(-(-c // (48 if spl == 0 else spl)) for c in (150, 37)) + 2
     for g in out:
         g.close()
 
@@ -190,3 +190,14 @@ def test_pipe_refused_configurations(sw2d_mod):
     with sw2d.Solver(rows=40, cols=40, dx=1.0, dy=1.0, precision=sw2d.PREC_F32, dt_mode=sw2d.DT_CFL, dt=0.01) as g:
         g.set_static(z)
         assert "steps_per_launch=1" in g.describe()
+
+
+def test_library_choice_of_steps_per_launch(sw2d_mod):
+    """steps_per_launch = 0: several iterations per launch where one wave
+    holds the grid in strips of at most 32 rows, one launch per iteration on
+    a 2048^2 grid (52-row strips)."""
+    import sw2d
+    for n, expect in ((512, "steps_per_launch=48"), (2048, "steps_per_launch=1")):
+        with sw2d.Solver(rows=n, cols=n, dx=5.0, dy=5.0, precision=sw2d.PREC_F32, dt_mode=sw2d.DT_FIXED, dt=0.4,
+                         kernel=sw2d.KERNEL_STREAM) as g:
+            assert expect in g.describe(), g.describe()
