@@ -31,15 +31,18 @@ int stream_out_cols() { return kStreamOut; }
 
 namespace {
 
-// The launch shape: strips of at most strip_h rows, split evenly; for the
-// pipelined launches the units go to warps in a scattered order (a
-// multiplier near 0.618 units, coprime with units).
-StreamShape stream_shape(int rows, int tiles_w, int strip_h, int units, bool scatter) {
+// The launch shape: ceil(rows / strip_h) strips, split evenly or with the
+// heights skewed (strip_rows); for the pipelined launches the units go to
+// warps in a scattered order (a multiplier near 0.618 units, coprime with
+// units).
+StreamShape stream_shape(int rows, int tiles_w, int strip_h, int units, bool scatter, int skew) {
     StreamShape sh;
+    std::memset(&sh, 0, sizeof(sh));
     sh.tiles_w = tiles_w;
     sh.strips = (rows + strip_h - 1) / strip_h;
     sh.units = units;
     sh.perm = 1;
+    sh.skew = skew;
     if (scatter && units > 2) {
         int p = (int)(units * 0.6180339887498949);
         if (p < 1) p = 1;
@@ -169,7 +172,7 @@ cudaError_t launch_stream_pipe(int variant, int nblocks, int tiles_w, int strip_
     pipe_plan_kernel<<<1, ((K + 31) / 32) * 32, 0, st>>>(G, F, clk, ctl, slot, plans, words, flags, units, K);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    const StreamShape sh = stream_shape(G.rows, tiles_w, strip_h, units, true);
+    const StreamShape sh = stream_shape(G.rows, tiles_w, strip_h, units, true, 0);
     PipeDesc P;
     P.plans = plans;
     P.words = words;
@@ -241,10 +244,10 @@ bool plane_map(CUtensorMap *m, const void *cell00, int rows, int pitch, bool u8)
 
 }  // namespace
 
-cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_h, int units, const GridDesc &G,
-                               const ForcingDesc &F, const StateBufs<float> &S, const Thr<float> &T, Clock *clk,
-                               const Control *ctl, int slot, cudaStream_t st) {
-    const StreamShape sh = stream_shape(G.rows, tiles_w, strip_h, units, false);
+cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_h, int units, int skew,
+                               const GridDesc &G, const ForcingDesc &F, const StateBufs<float> &S,
+                               const Thr<float> &T, Clock *clk, const Control *ctl, int slot, cudaStream_t st) {
+    const StreamShape sh = stream_shape(G.rows, tiles_w, strip_h, units, false, skew);
     // the general build carries the moving storm and the point sources
     const bool gen = F.rain_kind == RAIN_STORM || G.n_src > 0;
     cudaLaunchAttribute attr[1];

@@ -40,6 +40,7 @@ struct sw2d_handle {
     int tile_h = 16, tile_w = 32, nblocks = 0;
     bool stream_kernel = false;  // FP32 warp-streaming kernel instead of the tile kernel
     int strip_h = 0, stream_tiles_w = 0, stream_units = 0, variant = 0;
+    int strip_skew = 0;  // percent by which strip heights fall from the first strip to the last
     cudaStream_t stream = nullptr;
     void *h[2] = {nullptr, nullptr}, *um[2] = {nullptr, nullptr}, *vn[2] = {nullptr, nullptr};
     void *z = nullptr, *nman = nullptr;
@@ -145,7 +146,8 @@ StateBufs<Real> make_bufs(const sw2d_handle *h) {
 
 cudaError_t launch_one(sw2d_handle *h, int slot) {
     if (h->stream_kernel)
-        return launch_stream_step(h->variant, h->nblocks, h->stream_tiles_w, h->strip_h, h->stream_units, h->G, h->F,
+        return launch_stream_step(h->variant, h->nblocks, h->stream_tiles_w, h->strip_h, h->stream_units,
+                                  h->strip_skew, h->G, h->F,
                                   make_bufs<float>(h), make_thr<float>(h->cfg), h->d_clk, h->d_ctl, slot, h->stream);
     if (is_f64(h))
         return launch_step(h->tile_h, h->tile_w, h->nblocks, h->G, h->F, make_bufs<double>(h),
@@ -265,6 +267,11 @@ constexpr long long kMaxAutoStrip = 160;
 // Longest one-wave strip for which the library picks several iterations per
 // launch by itself (steps_per_launch = 0).
 constexpr int kAutoPipeMaxStrip = 32;
+
+// Skew of the strip heights for one launch per iteration over a full wave
+// (strip_rows in sw2d_stream.cuh): measured 0 / 10 / 20 / 35 % at 2048^2:
+// 80.7 / 80.6 / 79.4 / 84.0 us per iteration.
+constexpr int kStripSkew = 20;
 
 int auto_strip(int rows, int tiles_w, int variant, int device) {
     int sms = 0;
@@ -440,6 +447,17 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
         h->strip_h = sh;
         h->stream_units = h->stream_tiles_w * ((cfg->rows + sh - 1) / sh);
         h->nblocks = (h->stream_units + nw - 1) / nw;
+        if (h->pipe_k == 0) {
+            // one launch per iteration filling one wave of resident warps: the
+            // warp scheduler favours the CTAs launched first, so their strips
+            // get more rows (measured at 2048^2: 79.4 against 80.7 us)
+            int sms = 0;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg->device);
+            const long long resident = (long long)sms * stream_ctas_per_sm(h->variant) * nw;
+            const int strips = (cfg->rows + sh - 1) / sh;
+            if (h->stream_units <= resident && 10LL * h->stream_units >= 9 * resident && cfg->rows / strips >= 16)
+                h->strip_skew = kStripSkew;
+        }
         if (h->pipe_k > 0 && (cudaMalloc((void **)&h->d_plans, (size_t)h->pipe_k * sizeof(Plan)) != cudaSuccess ||
                               cudaMalloc((void **)&h->d_words, 2 * sizeof(unsigned)) != cudaSuccess ||
                               cudaMalloc((void **)&h->d_flags, 2 * (size_t)h->stream_units * sizeof(unsigned)) != cudaSuccess))
@@ -1015,10 +1033,13 @@ int sw2d_describe(const sw2d_handle *h, char *buf, int32_t n) {
             snprintf(buf, (size_t)n, "stream_pipe_kernel%s forcing=%s%s strip_h=%d units=%d ctas=%d steps_per_launch=%d",
                      std::strchr(stream_variant_name(h->variant), '<'), gen ? "storm/sources" : "uniform",
                      h->use_rainw ? "+rain_weights" : "", h->strip_h, h->stream_units, h->nblocks, h->pipe_k);
-        else
-            snprintf(buf, (size_t)n, "%s forcing=%s%s strip_h=%d units=%d ctas=%d steps_per_launch=1",
+        else {
+            char skew_s[32] = "";
+            if (h->strip_skew) snprintf(skew_s, sizeof(skew_s), " strip_skew=%d", h->strip_skew);
+            snprintf(buf, (size_t)n, "%s forcing=%s%s strip_h=%d units=%d ctas=%d steps_per_launch=1%s",
                      stream_variant_name(h->variant), gen ? "storm/sources" : "uniform",
-                     h->use_rainw ? "+rain_weights" : "", h->strip_h, h->stream_units, h->nblocks);
+                     h->use_rainw ? "+rain_weights" : "", h->strip_h, h->stream_units, h->nblocks, skew_s);
+        }
     }
     else
         snprintf(buf, (size_t)n, "step_kernel<%s,%d,%d> ctas=%d", is_f64(h) ? "double" : "float", h->tile_h,

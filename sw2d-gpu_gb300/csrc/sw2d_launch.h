@@ -67,9 +67,10 @@ int stream_warps(int variant);
 int stream_ctas_per_sm(int variant);
 const char *stream_variant_name(int variant);  // "stream_step_kernel<warps,minB,unroll>"  // resident CTAs per SM (occupancy), 0 on error
 cudaError_t prepare_stream_step(int variant);
-cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_h, int units, const GridDesc &G,
-                               const ForcingDesc &F, const StateBufs<float> &S, const Thr<float> &T, Clock *clk,
-                               const Control *ctl, int slot, cudaStream_t st);
+// skew: percent by which strip heights fall from the first strip to the last (0 = even).
+cudaError_t launch_stream_step(int variant, int nblocks, int tiles_w, int strip_h, int units, int skew,
+                               const GridDesc &G, const ForcingDesc &F, const StateBufs<float> &S,
+                               const Thr<float> &T, Clock *clk, const Control *ctl, int slot, cudaStream_t st);
 
 // The same kernel running several iterations per launch (fixed time step
 // only; sw2d_pipe.cuh): occupancy of its pipelined form, its limits, and the

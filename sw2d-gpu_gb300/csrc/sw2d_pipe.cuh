@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(NWARP * 32, MINB)
         const int ct = unit % SH.tiles_w, rs = unit / SH.tiles_w;
         const int nstrips = SH.strips;
         int r0, r1;
-        strip_rows(G.rows, SH.strips, rs, r0, r1);
+        strip_rows(G.rows, SH.strips, SH.skew, rs, r0, r1);
         r0 = __shfl_sync(0xffffffffu, r0, 0);  // the strip's rows, warp-uniform
         r1 = __shfl_sync(0xffffffffu, r1, 0);
         // lanes 0-8 but 4 watch the unit at (strip rs + lane/3 - 1, tile ct +

@@ -41,17 +41,36 @@ namespace sw2d {
 
 struct StreamShape {
     int tiles_w;  // column tiles of kStreamOut columns
-    int strips;   // strips per column tile: the rows split as evenly as whole rows allow
+    int strips;   // strips per column tile
     int units;    // tiles_w * strips
     int perm;     // warp w runs unit (w * perm) % units (perm coprime with units; 1 = in order)
+    int skew;     // percent by which strip heights fall from the first strip to the last (0 = even)
+    int pad[3];
 };
 
-// Rows [r0, r1) of strip rs when `rows` are split into `strips` strips whose
-// heights differ by at most one row (the first rows % strips are the longer).
-__device__ __forceinline__ void strip_rows(int rows, int strips, int rs, int &r0, int &r1) {
-    const int q = rows / strips, rem = rows - q * strips;
-    r0 = rs * q + min(rs, rem);
-    r1 = r0 + q + (rs < rem ? 1 : 0);
+// First row of strip k when strip heights follow the density
+// 1 + (skew/100)(1/2 - x) over x = k / strips: the boundary rounded to the
+// nearest row, in exact integer arithmetic.
+__device__ __forceinline__ int strip_start(int rows, int strips, int skew, int k) {
+    const long long R = rows, n = strips, kk = k;
+    return (int)((R * kk * 200 * n + skew * R * kk * (n - kk) + 100 * n * n) / (200 * n * n));
+}
+
+// Rows [r0, r1) of strip rs of `strips`.  skew == 0: heights differ by at
+// most one row (the first rows % strips are the longer).  skew > 0: heights
+// fall linearly from (1 + skew/200) to (1 - skew/200) of the mean, so that
+// the strips of the CTAs launched first -- which the warp scheduler favours
+// as the older warps -- carry more rows, and all warps of an SM finish at
+// about the same time.
+__device__ __forceinline__ void strip_rows(int rows, int strips, int skew, int rs, int &r0, int &r1) {
+    if (skew == 0) {
+        const int q = rows / strips, rem = rows - q * strips;
+        r0 = rs * q + min(rs, rem);
+        r1 = r0 + q + (rs < rem ? 1 : 0);
+    } else {
+        r0 = strip_start(rows, strips, skew, rs);
+        r1 = strip_start(rows, strips, skew, rs + 1);
+    }
 }
 
 // The unit warp w runs.
@@ -134,7 +153,7 @@ __device__ __forceinline__ void stream_step_body(const GridDesc &G, const Forcin
         V.dx = G.dx;
         V.dy = G.dy;
         int r0, r1;
-        strip_rows(G.rows, SH.strips, unit / SH.tiles_w, r0, r1);
+        strip_rows(G.rows, SH.strips, SH.skew, unit / SH.tiles_w, r0, r1);
         r0 = __shfl_sync(0xffffffffu, r0, 0);  // the strip's rows, warp-uniform (see above)
         r1 = __shfl_sync(0xffffffffu, r1, 0);
         stream_unit<UNR, RAINW, GEN, TMA>(V, unit % SH.tiles_w, r0, r1, lane, s_sr[wid],

@@ -54,6 +54,19 @@ def _strips_even(rows, strip_h):
     return out
 
 
+def _strip_start(rows, n, skew, k):
+    """strip_start of sw2d_stream.cuh in Python integers."""
+    return (rows * k * 200 * n + skew * rows * k * (n - k) + 100 * n * n) // (200 * n * n)
+
+
+def _strips_skew(rows, strip_h, skew=20):
+    """The single-scenario kernel's skewed split: ceil(rows / strip_h)
+    strips whose heights fall by `skew` percent from the first to the last."""
+    n = -(-rows // strip_h)
+    b = [_strip_start(rows, n, skew, k) for k in range(n + 1)]
+    return list(zip(b[:-1], b[1:]))
+
+
 def _strips_fixed(rows, strip_h):
     """The batched kernel's split: strips of strip_h rows, the last shorter."""
     return [(r0, min(r0 + strip_h, rows)) for r0 in range(0, rows, strip_h)]
@@ -100,6 +113,25 @@ def test_stream_windows_cover_once_and_stay_in_the_frame(rows, cols, strip_h):
     K = _consts()
     _check(rows, cols, strip_h, K, _strips_even)
     _check(rows, cols, strip_h, K, _strips_fixed)
+
+
+def test_skewed_split_matches_the_kernel_source_and_covers_the_rows():
+    """The model's skewed split is the kernel's formula; it starts at row 0,
+    ends at `rows`, has no empty strip and falls monotonically, for the
+    shapes the library skews (one full wave, mean height >= 16)."""
+    src = open(os.path.join(CSRC, "sw2d_stream.cuh")).read()
+    assert "return (int)((R * kk * 200 * n + skew * R * kk * (n - kk) + 100 * n * n) / (200 * n * n));" in src
+    api = open(os.path.join(CSRC, "sw2d_api.cu")).read()
+    skew = int(re.search(r"constexpr int kStripSkew = (\d+);", api).group(1))
+    K = _consts()
+    for rows, sh in ((2048, 52), (2048, 16), (4096, 103), (1000, 17), (16, 16), (33, 16), (8192, 137)):
+        sp = _strips_skew(rows, sh, skew)
+        assert sp[0][0] == 0 and sp[-1][1] == rows
+        assert all(a[1] == b[0] for a, b in zip(sp, sp[1:]))
+        hs = [r1 - r0 for r0, r1 in sp]
+        assert min(hs) >= 1 and all(x >= y - 1 for x, y in zip(hs, hs[1:]))  # falling, up to rounding
+        assert max(hs) <= round(sh * (1 + skew / 200)) + 1
+        _check(rows, 2049, sh, K, lambda r, s_: _strips_skew(r, s_, skew))
 
 
 def test_even_split_matches_the_kernel_source():
