@@ -1,18 +1,23 @@
-"""Autotuner for the FP32 kernels: tile shape, kernel build, launches per sync.
+"""Autotuner for the FP32 kernels: tile shape, kernel build, iterations per
+launch, launches per sync.
 
 For a grid-size class it times every candidate (strip height, kernel build)
 of the single-scenario streaming kernel on a wet synthetic catchment of that
-size and keeps the fastest; for batches it times the builds of the batched
-kernel with the CUDA-graph chunk (iterations replayed between host
-synchronisations) on a small ensemble.  Results are cached in a JSON file
-keyed by GPU name and size class (SW2D_AUTOTUNE_CACHE names the file), so a
-tuning run is paid once per machine.  Solver(**kw) and Batch(**kw) take the
-cached choice when the caller leaves the decomposition to the library
-(SW2D_AUTOTUNE=0 turns that off).
+size and keeps the fastest; under the reference's fixed time step it also
+times the iterations per launch (tune_fixed: one launch per iteration
+against 24, 48 and 96 iterations per cooperative launch); for batches it
+times the builds of the batched kernel with the CUDA-graph chunk
+(iterations replayed between host synchronisations) on a small ensemble.
+Results are cached in a JSON file keyed by GPU name and size class
+(SW2D_AUTOTUNE_CACHE names the file), so a tuning run is paid once per
+machine.  Solver(**kw) and Batch(**kw) take the cached choice when the
+caller leaves the decomposition to the library (SW2D_AUTOTUNE=0 turns that
+off).
 
     from sw2d import autotune
     best = autotune.tune(2048, 2048)          # {"strip_h": 52, "variant": 0, ...}
-    cfg = autotune.apply(cfg)                 # fills strip_h/variant from the cache
+    autotune.tune_fixed(1024, 1024)           # {"strip_h": 0, "variant": 0, "steps_per_launch": 48, ...}
+    cfg = autotune.apply(cfg)                 # fills strip_h/variant (and steps_per_launch) from the cache
     autotune.tune_batch()                     # {"variant": 0, "chunk": 24, ...}
 """
 from __future__ import annotations
@@ -46,6 +51,13 @@ def wave_strips(rows: int, cols: int, sms: int = 152, waves=(1, 2, 3, 4), warps_
 
 BATCH_VARIANTS = (0, 1, 2)
 BATCH_CLASS = "batch"
+STEPS_PER_LAUNCH = (1, 24, 48, 96)  # fixed time step: iterations per launch tried by tune_fixed
+FIXED_VARIANTS = (0, 2)
+
+
+def fixed_class(rows: int, cols: int) -> str:
+    """Cache key of the fixed-time-step choices of a size class."""
+    return "fixed|" + size_class(rows, cols)
 
 
 def default_cache_path() -> str:
@@ -121,16 +133,17 @@ def search(candidates, timer: Callable[[dict], float]):
     return {k: v for k, v in best.items() if k != "s_per_iter"}, table
 
 
-def _kernel_timer(rows, cols, device, iters):
+def _kernel_timer(rows, cols, device, iters, fixed=False):
     import sw2d
     from sw2d import scenarios as S
     s = S.catchment(rows, dx=5.0, seed=1, cols=cols)
     h0 = np.full((rows, cols), 0.005)
 
     def timer(c):
-        g = sw2d.Solver(rows=rows, cols=cols, dx=5.0, dy=5.0, precision=sw2d.PREC_F32, dt_mode=sw2d.DT_CFL, dt=1.0,
-                        cfl=0.5, south_open=1, kernel=sw2d.KERNEL_STREAM, strip_h=c["strip_h"],
-                        variant=c["variant"], device=device)
+        mode = dict(dt_mode=sw2d.DT_FIXED, dt=0.4) if fixed else dict(dt_mode=sw2d.DT_CFL, dt=1.0, cfl=0.5)
+        g = sw2d.Solver(rows=rows, cols=cols, dx=5.0, dy=5.0, precision=sw2d.PREC_F32, south_open=1,
+                        kernel=sw2d.KERNEL_STREAM, strip_h=c["strip_h"], variant=c["variant"],
+                        steps_per_launch=c.get("steps_per_launch", 1 if not fixed else 0), device=device, **mode)
         try:
             g.set_static(s["z"], s["n"])
             g.set_rain(sw2d.RAIN_STEP, [50.0], 3600.0)
@@ -162,12 +175,53 @@ def tune(rows: int, cols: int, device: int = 0, cache: Optional[Cache] = None, i
     return entry
 
 
+def fixed_candidates(rows: int, cols: int, best_one: Optional[dict] = None, variants=FIXED_VARIANTS,
+                     steps=STEPS_PER_LAUNCH):
+    """Candidates of tune_fixed: every build with the library's own strips
+    (strip_h 0: one wave for several iterations per launch) at each number of
+    iterations per launch, and the one-launch-per-iteration choice of tune()."""
+    cands = [{"strip_h": 0, "variant": v, "steps_per_launch": k} for v in variants for k in steps]
+    if best_one:
+        cands.append({"strip_h": int(best_one["strip_h"]), "variant": int(best_one["variant"]),
+                      "steps_per_launch": 1})
+    return cands
+
+
+def tune_fixed(rows: int, cols: int, device: int = 0, cache: Optional[Cache] = None, iters: int = 96,
+               variants=FIXED_VARIANTS, steps=STEPS_PER_LAUNCH, force: bool = False) -> dict:
+    """Best (strip_h, variant, steps_per_launch) under the fixed time step
+    for a rows x cols grid on this GPU (cached under fixed_class)."""
+    cache = cache or Cache()
+    gpu = f"{gpu_name(device)}|{TABLE_VERSION}"
+    hit = cache.get(gpu, fixed_class(rows, cols))
+    if hit and not force:
+        return hit
+    one = cache.get(gpu, size_class(rows, cols))
+    best, table = search(fixed_candidates(rows, cols, one, variants, steps),
+                         _kernel_timer(rows, cols, device, iters, fixed=True))
+    entry = {**best, "rows": rows, "cols": cols, "timings": table}
+    cache.put(gpu, fixed_class(rows, cols), entry)
+    return entry
+
+
 def apply(cfg, cache: Optional[Cache] = None, device: int = 0):
-    """Fills cfg.strip_h / cfg.variant from the cache (FP32 only); returns cfg."""
+    """Fills cfg.strip_h / cfg.variant from the cache (FP32 only), and under
+    the fixed time step cfg.steps_per_launch when tune_fixed has run for the
+    size class (its entry wins there); returns cfg."""
     import sw2d
     if cfg.precision != sw2d.PREC_F32:
         return cfg
-    hit = (cache or Cache()).get(f"{gpu_name(device)}|{TABLE_VERSION}", size_class(cfg.rows, cfg.cols))
+    c = cache or Cache()
+    gpu = f"{gpu_name(device)}|{TABLE_VERSION}"
+    hit = c.get(gpu, size_class(cfg.rows, cfg.cols))
+    if cfg.dt_mode == sw2d.DT_FIXED:
+        fixed = c.get(gpu, fixed_class(cfg.rows, cfg.cols))
+        if fixed:
+            cfg.strip_h = int(fixed["strip_h"])
+            cfg.variant = int(fixed["variant"])
+            if cfg.steps_per_launch == 0:
+                cfg.steps_per_launch = int(fixed["steps_per_launch"])
+            return cfg
     if hit:
         cfg.strip_h = int(hit["strip_h"])
         cfg.variant = int(hit["variant"])

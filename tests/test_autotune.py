@@ -108,3 +108,45 @@ def test_batch_tuning_picks_a_build_and_chunk(sw2d_mod, tmp_path, monkeypatch):
                 pass
             depth[v] = bt.field(sid)
     assert np.array_equal(depth[0], depth[1]) and np.array_equal(depth[0], depth[2])
+
+
+def test_fixed_candidates_and_apply(tmp_path):
+    """tune_fixed's candidates: every build at every iterations-per-launch
+    with the library's strips, plus the one-launch choice of tune(); apply
+    takes the fixed-step entry for a fixed-step config only, and leaves an
+    explicit steps_per_launch alone."""
+    import sw2d
+    from sw2d import autotune
+    c = autotune.fixed_candidates(1024, 1024, {"strip_h": 32, "variant": 2})
+    assert {"strip_h": 0, "variant": 0, "steps_per_launch": 48} in c
+    assert {"strip_h": 32, "variant": 2, "steps_per_launch": 1} in c
+    assert len(c) == len(autotune.FIXED_VARIANTS) * len(autotune.STEPS_PER_LAUNCH) + 1
+    cache = autotune.Cache(str(tmp_path / "t.json"))
+    gpu = f"{autotune.gpu_name(0)}|{autotune.TABLE_VERSION}"
+    cache.put(gpu, autotune.size_class(1024, 1024), {"strip_h": 32, "variant": 2})
+    cache.put(gpu, autotune.fixed_class(1024, 1024), {"strip_h": 0, "variant": 0, "steps_per_launch": 96})
+    cfl = sw2d.default_config(rows=1024, cols=1024, precision=sw2d.PREC_F32, dt_mode=sw2d.DT_CFL)
+    autotune.apply(cfl, cache=cache)
+    assert (cfl.strip_h, cfl.variant, cfl.steps_per_launch) == (32, 2, 0)
+    fx = sw2d.default_config(rows=1024, cols=1024, precision=sw2d.PREC_F32, dt_mode=sw2d.DT_FIXED)
+    autotune.apply(fx, cache=cache)
+    assert (fx.strip_h, fx.variant, fx.steps_per_launch) == (0, 0, 96)
+    fx1 = sw2d.default_config(rows=1024, cols=1024, precision=sw2d.PREC_F32, dt_mode=sw2d.DT_FIXED,
+                              steps_per_launch=1)
+    autotune.apply(fx1, cache=cache)
+    assert fx1.steps_per_launch == 1
+
+
+@pytest.mark.gpu
+def test_tune_fixed_on_gpu(sw2d_mod, tmp_path):
+    """A small real tuning run under the fixed time step picks one of its
+    candidates, and a fixed-step Solver without a decomposition takes it."""
+    from sw2d import autotune
+    cache = autotune.Cache(str(tmp_path / "t.json"))
+    best = autotune.tune_fixed(256, 256, cache=cache, iters=48, variants=(0,), steps=(1, 48))
+    assert best["steps_per_launch"] in (1, 48) and best["variant"] == 0
+    cfg = sw2d_mod.default_config(rows=256, cols=256, precision=sw2d_mod.PREC_F32, dt_mode=sw2d_mod.DT_FIXED, dt=0.1)
+    autotune.apply(cfg, cache=cache)
+    g = sw2d_mod.Solver(cfg)
+    assert f"steps_per_launch={best['steps_per_launch']}" in g.describe()
+    g.close()
