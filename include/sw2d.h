@@ -103,7 +103,8 @@ typedef struct {
                                as one launch per iteration); 1 = one launch per iteration;
                                0 = the library's choice (48 where one wave of resident warps
                                holds the grid in strips of at most 32 rows -- grids up to
-                               about 1600^2 --, else 1).  At most 1024; values >= 2 with
+                               about 1600^2 -- and while neither a moving storm nor point
+                               sources are set, else 1).  At most 1024; values >= 2 with
                                SW2D_DT_CFL or another kernel are SW2D_ERR_INVALID_ARG. */
 } sw2d_config;
 

@@ -67,6 +67,8 @@ struct sw2d_handle {
     // iterations per launch (0 = one launch per iteration), the plan table,
     // its run count and abort word, and the per-unit progress counters
     int pipe_k = 0;
+    bool pipe_auto = false;    // pipe_k is the library's choice (steps_per_launch = 0)
+    bool fold_needed = false;  // one-iteration launches left a budget fold to do (read_clock)
     Plan *d_plans = nullptr;
     unsigned *d_words = nullptr;
     unsigned *d_flags = nullptr;
@@ -156,6 +158,17 @@ cudaError_t launch_one(sw2d_handle *h, int slot) {
                        make_thr<float>(h->cfg), h->d_clk, h->d_ctl, slot, h->stream);
 }
 
+// Whether advance runs several iterations per launch now: the pipelined form
+// with the storm or point sources compiled in spills at 96 registers and
+// measured 0.86-0.94x one launch per iteration on 256^2 to 1024^2, so the
+// library's own choice of it (not one the caller asked for) stands down
+// while that forcing is set.
+bool pipe_now(const sw2d_handle *h) {
+    if (h->pipe_k <= 0) return false;
+    const bool gen = h->F.rain_kind == RAIN_STORM || h->G.n_src > 0;
+    return !(h->pipe_auto && gen);
+}
+
 int validate(const sw2d_config *c, std::string *why) {
     if (!c) return *why = "config is null", 0;
     if (c->rows < 1 || c->cols < 1) return *why = "rows and cols must be >= 1", 0;
@@ -193,10 +206,11 @@ int read_clock(sw2d_handle *h) {
     // the streaming kernel leaves the budget fold of the slot its last
     // launch wrote to the next launch (finish_cta_deferred_warp): fold it
     // here (a fold is idempotent)
-    if (h->stream_kernel && h->pipe_k == 0 && h->have_state) {
+    if (h->stream_kernel && h->fold_needed && h->have_state) {
         fold_kernel<<<1, 32, 0, h->stream>>>(h->d_clk, slot, (slot + 2) % 3);
         CK(h, cudaGetLastError());
         h->kernels++;
+        h->fold_needed = false;
     }
     CK(h, cudaMemcpyAsync(h->h_clk, h->d_clk + slot, sizeof(Clock), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
@@ -437,6 +451,7 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
             const bool worth = cfg->steps_per_launch > 1 || psh <= kAutoPipeMaxStrip;
             if (tall && worth && units > 0 && units <= resident) {
                 h->pipe_k = cfg->steps_per_launch > 1 ? cfg->steps_per_launch : kChunk;
+                h->pipe_auto = cfg->steps_per_launch == 0;
                 sh = psh;
             } else if (cfg->steps_per_launch > 1) {
                 h->err = "steps_per_launch > 1: the units must fit one wave of resident warps, in strips of at least 8 rows";
@@ -628,6 +643,7 @@ int sw2d_set_state(sw2d_handle *h, const double *depth, const double *um, const 
                           &h->d_clk[0].cmax_bits, h->stream));
     h->launches = 0;
     h->kernels = 0;
+    h->fold_needed = false;
     h->have_state = true;
     int rc = read_clock(h);
     if (rc) return rc;
@@ -764,7 +780,7 @@ int sw2d_advance(sw2d_handle *h, int64_t max_steps, double t_end, int64_t *steps
         std::memcpy(&cmax, &h->clock.cmax_bits, sizeof(double));
         if (!decide_step(h->clock.t, cmax, h->clock.steps, ctl, h->G, &dtn)) break;
         const long long remaining = ctl.step_limit - h->clock.steps;
-        if (h->pipe_k > 0) {
+        if (pipe_now(h)) {
             // up to pipe_k iterations in one cooperative launch (the plan
             // kernel stops it at step_limit and t_end)
             CK(h, launch_stream_pipe(h->variant, h->nblocks, h->stream_tiles_w, h->strip_h, h->stream_units, h->G,
@@ -781,12 +797,14 @@ int sw2d_advance(sw2d_handle *h, int64_t max_steps, double t_end, int64_t *steps
             CK(h, cudaGraphLaunch(h->graph, h->stream));
             h->launches += kChunk;
             h->kernels += kChunk;
+            h->fold_needed = h->stream_kernel;
         } else {
             const long long n = ((remaining + 2) / 3) * 3;
             for (long long m = 0; m < n; m++) {
                 CK(h, launch_one(h, (int)((h->launches) % 3)));
                 h->launches++;
                 h->kernels++;
+                h->fold_needed = h->stream_kernel;
             }
         }
         int rc = read_clock(h);
@@ -999,6 +1017,7 @@ int sw2d_checkpoint_load(sw2d_handle *h, const void *buf, int64_t bytes) {
     CK(h, cudaStreamSynchronize(h->stream));
     h->launches = 0;
     h->kernels = 0;
+    h->fold_needed = false;
     h->clock = c;
     h->volume0 = hd.volume0;
     h->have_state = true;
@@ -1029,7 +1048,7 @@ int sw2d_describe(const sw2d_handle *h, char *buf, int32_t n) {
         // the forcing build the launcher picks (step_f32.cu): storm and point
         // sources, per-cell rain factors, or neither
         const bool gen = h->F.rain_kind == RAIN_STORM || h->G.n_src > 0;
-        if (h->pipe_k > 0)
+        if (pipe_now(h))
             snprintf(buf, (size_t)n, "stream_pipe_kernel%s forcing=%s%s strip_h=%d units=%d ctas=%d steps_per_launch=%d",
                      std::strchr(stream_variant_name(h->variant), '<'), gen ? "storm/sources" : "uniform",
                      h->use_rainw ? "+rain_weights" : "", h->strip_h, h->stream_units, h->nblocks, h->pipe_k);

@@ -195,9 +195,26 @@ def test_pipe_refused_configurations(sw2d_mod):
 def test_library_choice_of_steps_per_launch(sw2d_mod):
     """steps_per_launch = 0: several iterations per launch where one wave
     holds the grid in strips of at most 32 rows, one launch per iteration on
-    a 2048^2 grid (52-row strips)."""
+    a 2048^2 grid (52-row strips), and one launch per iteration while a storm
+    or point sources are set (the form that carries them spills in the
+    pipelined kernel) unless the caller asked for several; the results are
+    the same bits either way."""
     import sw2d
     for n, expect in ((512, "steps_per_launch=48"), (2048, "steps_per_launch=1")):
         with sw2d.Solver(rows=n, cols=n, dx=5.0, dy=5.0, precision=sw2d.PREC_F32, dt_mode=sw2d.DT_FIXED, dt=0.4,
                          kernel=sw2d.KERNEL_STREAM) as g:
             assert expect in g.describe(), g.describe()
+    rows, cols = 120, 200
+    s, z = _catchment(rows, cols, 43)
+    out = []
+    for k in (0, 16):
+        g = _solver(sw2d_mod, rows, cols, 5.0, z, s["h0"], spl=k, dt=0.4, south_open=1, manning=0.05)
+        assert "stream_pipe_kernel" in g.describe()
+        g.set_storm(150.0, 0.0, 0.0, 2.0, 1.0, 400.0)
+        d = g.describe()
+        assert ("stream_pipe_kernel" in d) == (k == 16), d
+        assert g.advance(100) == 100
+        out.append(g)
+    _same(*out)
+    for g in out:
+        g.close()
