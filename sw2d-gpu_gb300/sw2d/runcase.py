@@ -7,7 +7,9 @@ ncu summaries under profiles/ were made with:
 
 The catchment (seeded, see scenarios.catchment) starts from a uniform 5 mm
 film so that every cell does the full update; rain 50 mm/h, open south edge,
-CFL 0.5.  Three warm-up iterations, then --iters timed iterations.
+CFL 0.5 (or the reference's fixed half step with --fixed-dt, and
+--steps-per-launch iterations per launch).  Three warm-up iterations, then
+--iters timed iterations.
 """
 import argparse
 import os
@@ -32,13 +34,18 @@ def main():
     ap.add_argument("--variant", type=int, default=0)
     ap.add_argument("--tile", type=int, nargs=2, default=(0, 0))
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--fixed-dt", type=float, default=0.0,
+                    help="the reference's time-step rule with this half step [s] instead of CFL 0.5")
+    ap.add_argument("--steps-per-launch", type=int, default=0, help="0 = the library's choice")
     a = ap.parse_args()
     n = a.size
     prec = sw2d.PREC_F32 if a.precision == "f32" else sw2d.PREC_F64
     s = S.catchment(n, dx=5.0, seed=a.seed)
-    g = sw2d.Solver(rows=n, cols=n, dx=5.0, dy=5.0, precision=prec, dt_mode=sw2d.DT_CFL, dt=1.0, cfl=0.5,
-                    south_open=1, kernel=a.kernel, strip_h=a.strip_h, variant=a.variant, tile_h=a.tile[0],
-                    tile_w=a.tile[1])
+    mode = dict(dt_mode=sw2d.DT_FIXED, dt=a.fixed_dt) if a.fixed_dt > 0 else dict(dt_mode=sw2d.DT_CFL, dt=1.0,
+                                                                                      cfl=0.5)
+    g = sw2d.Solver(rows=n, cols=n, dx=5.0, dy=5.0, precision=prec, south_open=1, kernel=a.kernel,
+                    strip_h=a.strip_h, variant=a.variant, tile_h=a.tile[0], tile_w=a.tile[1],
+                    steps_per_launch=a.steps_per_launch, **mode)
     g.set_static(s["z"], s["n"])
     g.set_rain(sw2d.RAIN_STEP, [50.0], 3600.0)
     g.set_state(np.full((n, n), 0.005))
