@@ -97,7 +97,8 @@ typedef struct {
     int32_t variant;        /* streaming-kernel build (occupancy / unrolling), 0 = default;
                                chosen by the autotuner */
     int32_t steps_per_launch; /* iterations per kernel launch of the FP32 streaming kernel
-                               under SW2D_DT_FIXED: K >= 2 runs K iterations per cooperative
+                               (the reference launches nine kernels per iteration,
+                               cu:1256-1336) under SW2D_DT_FIXED: K >= 2 runs K iterations per cooperative
                                launch, each warp starting its next iteration as soon as the
                                units around it have finished theirs (same state, bit for bit,
                                as one launch per iteration); 1 = one launch per iteration;
@@ -198,7 +199,11 @@ int sw2d_set_point_sources(sw2d_handle *h, const int32_t *cells, int32_t n_src, 
 /* Runs iterations of the solver loop until max_steps iterations are done or
  * the end-time condition fails (FIXED: t + dt <= t_end as in cu:1256; CFL:
  * t < t_end, last step clipped to land on t_end).  *steps_done (nullable)
- * receives the count.  Replaces the while loop cu:1256-1336. */
+ * receives the count.  Replaces the while loop cu:1256-1336, which launches
+ * nine kernels per iteration; here each iteration is one launch of the fused
+ * step kernel, or cfg.steps_per_launch iterations share one cooperative
+ * launch.  Returns SW2D_ERR_NONFINITE when a NaN/Inf was produced and
+ * SW2D_ERR_TIMEOUT when a bounded wait inside such a launch gave up. */
 int sw2d_advance(sw2d_handle *h, int64_t max_steps, double t_end, int64_t *steps_done);
 
 /* Copies a field of the current state to host memory (size per field enum).
@@ -239,7 +244,7 @@ int sw2d_launch_count(sw2d_handle *h, int64_t *launches);
 
 /* One line naming the step kernel build and the decomposition the handle
  * runs, e.g. "stream_step_kernel<2,10,2> forcing=uniform strip_h=52 units=3040
- * ctas=1520 steps_per_launch=1"
+ * ctas=1520 steps_per_launch=1 strip_skew=20"
  * (written NUL-terminated, truncated to `n` bytes).  No reference
  * counterpart: the reference's launch shape is fixed at cu:1222-1235. */
 int sw2d_describe(const sw2d_handle *h, char *buf, int32_t n);
