@@ -217,6 +217,12 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
     T.gt_th = gt_th;
     T.ge_th = ge_th;
     T.gt_evmin = gt_ev;
+    // continuity (cu:603-665) in the uniform-rain form (no storm, sources or
+    // rain factors): -dt2/dx, -dt2/dy, and the forcing dt2 (rr pct - ev) by
+    // whether the old depth is above EV_WL_min, at t (f0) and t + dt (f1)
+    const float ndx = -dt2 * rdx, ndy = -dt2 * rdy;
+    const float f0_hi = dt2 * (u_rr0 * pct_hi - u_ev0), f0_lo = dt2 * (u_rr0 * pct_lo);
+    const float f1_hi = dt2 * (u_rr1 * pct_hi - u_ev1), f1_lo = dt2 * (u_rr1 * pct_lo);
     const float sqrt_g = sqrtf(g);
     // |q/h| + sqrt(g h) with one reciprocal square root: r = 1/sqrt(h)
     auto wave_speed = [&](float q, float h) {
@@ -511,7 +517,12 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
             const float ql = nsrc ? source_at(r - 2, false) : 0.f;
             float rr = storm ? storm_rate(r - 2, on0, sx0, sy0) : u_rr0;
             if (RAINW) rr = rr * Win[(r - 2) * pitch + gj];
-            hs_2 = fmaxf(ho - dt2 * ((rum_1 - rum_2) * rdx + (rvnE_2 - rvn_2) * rdy - ql - rr * pct + evapo), 0.f);
+            if constexpr (!GEN && !RAINW) {  // the cell's forcing is one select of per-warp values
+                hs_2 = fmaxf(ho + ((rum_1 - rum_2) * ndx + (rvnE_2 - rvn_2) * ndy) + (hi ? f0_hi : f0_lo), 0.f);
+            } else {
+                hs_2 = fmaxf(ho - dt2 * ((rum_1 - rum_2) * rdx + (rvnE_2 - rvn_2) * rdy - ql - rr * pct + evapo),
+                             0.f);
+            }
         }
 
         // ---- row r-3: dry-cell fix (cu:695-725) and final depth ----
@@ -545,7 +556,12 @@ __device__ __forceinline__ void stream_unit(const StreamView &V, const int ct, c
             // behind its FP64 budget.  The fast two-sum is exact here: an update
             // larger than the depth either drains the cell (clamped below) or
             // fills it from 0, and the remainder is below an ulp of the depth.
-            const float d = __fmul_rn(-dt2, (us - un) * rdx + (ve - vw) * rdy - ql1 - rr1 * pct1 + ev1);
+            float d;
+            if constexpr (!GEN && !RAINW) {
+                d = (us - un) * ndx + (ve - vw) * ndy + (hi ? f1_hi : f1_lo);
+            } else {
+                d = __fmul_rn(-dt2, (us - un) * rdx + (ve - vw) * rdy - ql1 - rr1 * pct1 + ev1);
+            }
             float s, e, hn, rn;
             fast_two_sum(ho, d, s, e);
             fast_two_sum(s, __fadd_rn(res3, e), hn, rn);
