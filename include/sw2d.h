@@ -94,8 +94,10 @@ typedef struct {
     int32_t tile_h, tile_w; /* core tile of the shared-memory step kernel, 0 = default */
     int32_t kernel;         /* SW2D_KERNEL_*: which step kernel (AUTO picks per precision) */
     int32_t strip_h;        /* rows per warp of the FP32 streaming kernel, 0 = auto */
-    int32_t variant;        /* streaming-kernel build (occupancy / unrolling), 0 = default;
-                               chosen by the autotuner */
+    int32_t variant;        /* streaming-kernel build (occupancy / unrolling), 0..6, 0 = default;
+                               chosen by the autotuner among 0..5; 6 stages the rows in shared
+                               memory by TMA (uniform forcing; the other forms run build 0);
+                               every build gives the same state bits */
     int32_t steps_per_launch; /* iterations per kernel launch of the FP32 streaming kernel
                                (the reference launches nine kernels per iteration,
                                cu:1256-1336) under SW2D_DT_FIXED: K >= 2 runs K iterations per cooperative
