@@ -303,6 +303,73 @@ int sw2d_batch_get_stream(sw2d_batch *b, void **stream);
 int sw2d_batch_launch_count(sw2d_batch *b, int64_t *launches);
 const char *sw2d_batch_last_error(const sw2d_batch *b);
 
+/* ---------------------------------------------------------------------------
+ * Continuous batching (extension): a serving loop over one batch, for a host
+ * program that receives flood scenarios over time.
+ *
+ * Requests are submitted at any time.  Each sw2d_server_step admits the
+ * waiting requests in submission order while the batch has a free scenario
+ * slot (max_scenarios) and the request's device footprint
+ * (sw2d_batch_scenario_bytes) fits the batch's max_bytes -- a request that
+ * does not fit keeps its place and smaller ones behind it may pass it --,
+ * advances every resident request by launches_per_step iterations, and
+ * retires those whose end time is reached: their budgets (and, with
+ * keep_depth, their depth raster) are copied to host memory and their device
+ * memory is released at once.  A request advances bit for bit as it would
+ * alone in an FP32 handle.  A request the batch refuses at admission (an
+ * invalid argument or its memory) fails alone.  A server is not
+ * thread-safe.
+ * ------------------------------------------------------------------------- */
+typedef struct sw2d_server sw2d_server;
+
+typedef struct {
+    sw2d_batch_config batch;   /* the batch: device, scenario slots, memory budget, kernel build */
+    int32_t launches_per_step; /* iterations per sw2d_server_step, >= 1 (24) */
+    int32_t keep_depth;        /* 1: keep each finished request's depth raster until released (1) */
+    int32_t reserved[2];
+} sw2d_server_config;
+
+enum {
+    SW2D_REQ_UNKNOWN = 0,   /* never submitted, or released */
+    SW2D_REQ_PENDING = 1,   /* waiting for a slot and memory */
+    SW2D_REQ_RUNNING = 2,   /* resident in the batch */
+    SW2D_REQ_DONE = 3,      /* end time reached; results held until released */
+    SW2D_REQ_FAILED = 4,    /* refused at admission (sw2d_server_request_error) */
+    SW2D_REQ_CANCELLED = 5
+};
+
+int sw2d_server_config_init(sw2d_server_config *cfg);
+int sw2d_server_create(const sw2d_server_config *cfg, sw2d_server **out);
+int sw2d_server_destroy(sw2d_server *s);
+/* Queues a request; the arguments are those of sw2d_batch_add.  The rasters
+ * and the rain series are copied, so the caller's buffers may be reused on
+ * return.  A request whose footprint exceeds the whole memory budget is
+ * SW2D_ERR_INVALID_ARG.  *request: its id, 1, 2, ... */
+int sw2d_server_submit(sw2d_server *s, const sw2d_config *cfg, const double *z, const double *manning,
+                       const double *depth, int32_t rain_kind, const double *rain, int32_t n_rain, double rain_dt,
+                       double t_end, int32_t *request);
+/* One round -- admit, advance, retire -- and wait for it.  *pending and
+ * *running (either may be NULL): the requests waiting and resident after it. */
+int sw2d_server_step(sw2d_server *s, int32_t *pending, int32_t *running);
+/* State (SW2D_REQ_*), simulated time and iterations of a request: as of the
+ * last step while it runs, final once done.  t and steps may be NULL. */
+int sw2d_server_poll(const sw2d_server *s, int32_t request, int32_t *state, double *t, int64_t *steps);
+/* Results of a finished (SW2D_REQ_DONE) request: its FP64 budgets, and its
+ * depth raster (rows x cols, kept with keep_depth). */
+int sw2d_server_get_budget(const sw2d_server *s, int32_t request, sw2d_budget *out);
+int sw2d_server_get_depth(const sw2d_server *s, int32_t request, double *out);
+/* Withdraws a pending or running request (a running one leaves the batch
+ * and its memory is released); SW2D_ERR_INVALID_ARG otherwise. */
+int sw2d_server_cancel(sw2d_server *s, int32_t request);
+/* Forgets a finished, failed or cancelled request and its results. */
+int sw2d_server_release(sw2d_server *s, int32_t request);
+/* Device bytes held by the resident requests. */
+int sw2d_server_bytes_in_use(const sw2d_server *s, int64_t *bytes);
+int sw2d_server_get_batch(sw2d_server *s, sw2d_batch **batch);  /* the underlying batch (stream, launch count) */
+const char *sw2d_server_last_error(const sw2d_server *s);
+/* Why a failed request was refused ("" for any other). */
+const char *sw2d_server_request_error(const sw2d_server *s, int32_t request);
+
 /* Largest grid sw2d_volume_noalloc accepts: 8192 x 8192 cells. */
 #define SW2D_NOALLOC_MAX_CELLS (8192LL * 8192LL)
 

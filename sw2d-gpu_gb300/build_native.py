@@ -35,6 +35,8 @@ UNITS = {
     "sw2d_noalloc.cu": ["--fmad=false"],
     # same flags as step_f32.cu: a batched scenario advances bit for bit as alone
     "sw2d_batch.cu": ["--use_fast_math"],
+    # the serving loop over the batch: host C++ only
+    "sw2d_serve.cpp": [],
 }
 
 
@@ -64,7 +66,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(item):
         src, flags = item
-        obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
         cmd = [cc, *ARCH, *COMMON, *flags, "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)

@@ -432,8 +432,12 @@ int sw2d_batch_add(sw2d_batch *b, const sw2d_config *cfg, const double *z, const
     BCK(b, cudaMemcpyAsync(b->d_status + slot, &s0, sizeof(s0), cudaMemcpyHostToDevice, b->stream));
     h.active = true;
     int rc = upload_units(b);  // synchronises: the host-side sources above are safe to reuse
-    if (rc) {
+    if (rc) {  // the unit table is full: the scenario is not admitted and its memory goes back
         h.active = false;
+        cudaFreeAsync(h.block, b->stream);
+        h.block = nullptr;
+        b->bytes_in_use -= (int64_t)h.bytes;
+        h.bytes = 0;
         return rc;
     }
     *id = slot;

@@ -55,6 +55,16 @@ class BatchConfig(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [
+        ("batch", BatchConfig), ("launches_per_step", C.c_int32), ("keep_depth", C.c_int32),
+        ("reserved", C.c_int32 * 2),
+    ]
+
+
+REQ_UNKNOWN, REQ_PENDING, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = range(6)
+
+
 class SW2DError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__(f"{msg} (status {status})")
@@ -108,6 +118,22 @@ _SIGS = {
     "sw2d_batch_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "sw2d_batch_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "sw2d_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "sw2d_server_config_init": (C.c_int, [C.POINTER(ServerConfig)]),
+    "sw2d_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
+    "sw2d_server_destroy": (C.c_int, [C.c_void_p]),
+    "sw2d_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Config), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                     C.c_void_p, C.c_int32, C.c_double, C.c_double, C.POINTER(C.c_int32)]),
+    "sw2d_server_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "sw2d_server_poll": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                                   C.POINTER(C.c_int64)]),
+    "sw2d_server_get_budget": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(Budget)]),
+    "sw2d_server_get_depth": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "sw2d_server_cancel": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sw2d_server_release": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sw2d_server_bytes_in_use": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "sw2d_server_get_batch": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "sw2d_server_last_error": (C.c_char_p, [C.c_void_p]),
+    "sw2d_server_request_error": (C.c_char_p, [C.c_void_p, C.c_int32]),
 }
 
 
@@ -474,4 +500,113 @@ class Batch:
         """Batch-kernel launches issued so far."""
         v = C.c_int64()
         self._check(load().sw2d_batch_launch_count(self._h, C.byref(v)), "sw2d_batch_launch_count")
+        return int(v.value)
+
+
+def server_config(**kw) -> ServerConfig:
+    """A ServerConfig from the library's defaults; batch fields (device, max_scenarios, max_bytes, chunk,
+    variant, ...) and the server's own (launches_per_step, keep_depth) as keywords."""
+    c = ServerConfig()
+    load().sw2d_server_config_init(C.byref(c))
+    for k, v in kw.items():
+        if hasattr(c.batch, k):
+            setattr(c.batch, k, v)
+        elif hasattr(c, k) and k != "batch":
+            setattr(c, k, v)
+        else:
+            raise AttributeError(f"sw2d_server_config has no field {k}")
+    return c
+
+
+class ServerHandle:
+    """The native serving loop (C-ABI sw2d_server_*): continuous batching of FP32 scenarios over one batch --
+    admission in submission order by free slot and device-memory footprint, one tick per step, retirement
+    with results copied to the host."""
+
+    def __init__(self, cfg: ServerConfig | None = None, **kw):
+        L = load()
+        self.cfg = cfg if cfg is not None else server_config(**kw)
+        h = C.c_void_p()
+        st = L.sw2d_server_create(C.byref(self.cfg), C.byref(h))
+        if st != OK:
+            raise SW2DError(st, "sw2d_server_create failed: " + L.sw2d_status_string(st).decode())
+        self._h = h
+        self.shapes = {}
+
+    def _check(self, st, what):
+        if st != OK:
+            raise SW2DError(st, f"{what}: {load().sw2d_server_last_error(self._h).decode()}")
+
+    def close(self):
+        """Frees the server, its batch and every resident request's device memory; safe to call twice."""
+        if getattr(self, "_h", None):
+            load().sw2d_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, cfg: Config, z, depth, manning=None, rain_kind=RAIN_NONE, rain=None, rain_dt=1.0, t_end=1e300):
+        """Queues one FP32 CFL scenario (arguments as Batch.add); returns its request id."""
+        r, c = cfg.rows, cfg.cols
+        z = _f64(z, (r, c))
+        d = _f64(depth, (r, c))
+        n = _f64(manning, (r, c)) if manning is not None else None
+        rs = _f64(np.atleast_1d(rain)) if rain is not None else None
+        rid = C.c_int32()
+        self._check(load().sw2d_server_submit(self._h, C.byref(cfg), _p(z), _p(n), _p(d), int(rain_kind), _p(rs),
+                                              0 if rs is None else rs.size, float(rain_dt), float(t_end),
+                                              C.byref(rid)), "sw2d_server_submit")
+        self.shapes[rid.value] = (r, c)
+        return rid.value
+
+    def step(self):
+        """One round (admit, advance, retire); returns (pending, running) after it."""
+        p, r = C.c_int32(), C.c_int32()
+        self._check(load().sw2d_server_step(self._h, C.byref(p), C.byref(r)), "sw2d_server_step")
+        return p.value, r.value
+
+    def poll(self, rid):
+        """{state, t, steps} of request rid (state: REQ_*)."""
+        st, t, n = C.c_int32(), C.c_double(), C.c_int64()
+        self._check(load().sw2d_server_poll(self._h, int(rid), C.byref(st), C.byref(t), C.byref(n)),
+                    "sw2d_server_poll")
+        return {"state": st.value, "t": t.value, "steps": int(n.value)}
+
+    def budget(self, rid):
+        """The FP64 budgets of a finished request, as Solver.budget."""
+        b = Budget()
+        self._check(load().sw2d_server_get_budget(self._h, int(rid), C.byref(b)), "sw2d_server_get_budget")
+        return {k: getattr(b, k) for k, _ in Budget._fields_ if k != "reserved"}
+
+    def depth(self, rid):
+        """The final depth raster of a finished request (kept with keep_depth)."""
+        out = np.empty(self.shapes[rid])
+        self._check(load().sw2d_server_get_depth(self._h, int(rid), _p(out)), "sw2d_server_get_depth")
+        return out
+
+    def cancel(self, rid):
+        """Withdraws a pending or running request."""
+        self._check(load().sw2d_server_cancel(self._h, int(rid)), "sw2d_server_cancel")
+
+    def release(self, rid):
+        """Forgets a finished, failed or cancelled request."""
+        self._check(load().sw2d_server_release(self._h, int(rid)), "sw2d_server_release")
+        self.shapes.pop(rid, None)
+
+    def request_error(self, rid):
+        return load().sw2d_server_request_error(self._h, int(rid)).decode()
+
+    def bytes_in_use(self):
+        v = C.c_int64()
+        self._check(load().sw2d_server_bytes_in_use(self._h, C.byref(v)), "sw2d_server_bytes_in_use")
         return int(v.value)
