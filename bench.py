@@ -597,13 +597,19 @@ def run_served(sw2d, dev, args):
     m = min(args.serve_fp64_sample, len(order))
     sample = {order[int(round(i * (len(order) - 1) / max(m - 1, 1)))][1] for i in range(m)}
     from sw2d import autotune
-    tick = autotune.apply_batch(sw2d.batch_config(device=dev)).chunk  # a tick is one graph replay
-    srv = serve.Server(lambda: sw2d.Batch(device=dev, max_scenarios=len(reqs) + 8, max_bytes=budget),
-                       bytes_of=lambda r: sw2d.batch_scenario_bytes(r.cfg, 3, True), max_bytes=budget,
-                       launches_per_tick=tick, keep_results=lambda r: r.rid in sample)
+    bc = autotune.apply_batch(sw2d.batch_config(device=dev))  # the batch build and graph chunk
+    tick = bc.chunk  # a tick is one graph replay
+    # the library's own serving loop (sw2d_server_*): admission by device
+    # footprint and free slots, one tick per step, retirement with the
+    # results copied to the host; Python submits each request at its arrival
+    srv = serve.NativeServer(lambda: sw2d.ServerHandle(device=dev, max_scenarios=len(reqs) + 8, max_bytes=budget,
+                                                       chunk=bc.chunk, variant=bc.variant, launches_per_step=tick,
+                                                       keep_depth=1),
+                             keep_results=lambda r: r.rid in sample)
     st = srv.run(reqs, timeout=600.0)
-    srv.batch.close()
-    st.update({"rate_per_s": args.serve_rate, "memory_budget_gb": args.serve_gb, "launches_per_tick": tick})
+    srv.close()
+    st.update({"rate_per_s": args.serve_rate, "memory_budget_gb": args.serve_gb, "launches_per_tick": tick,
+               "loop": "sw2d_server_* (library)"})
     # the plain sequential FP64 path on the same request set: the sampled
     # requests run alone in FP64 (measured: their time and their error); every
     # other request's FP64 time is its served cell-updates at the FP64 rate

@@ -15,8 +15,11 @@ time.  Between ticks it
 Nothing here touches the numerics: each scenario advances exactly as it
 would alone (per-scenario clocks and CFL steps in the batched kernel).
 
-The backend is injected (`batch_factory`), so the scheduling logic is
-tested on the host with a fake batch.
+`Server` schedules in Python over a `Batch`; its backend is injected
+(`batch_factory`), so the scheduling logic is tested on the host with a fake
+batch.  `NativeServer` runs the same policy through the library's own loop
+(`ServerHandle`, the C ABI's sw2d_server_*) and keeps only the arrival clock
+and the statistics here.
 """
 from __future__ import annotations
 
@@ -187,28 +190,135 @@ class Server:
         return self.stats()
 
     def stats(self):
-        if not self.done:
-            return {"requests": 0}
-        served = [r for r in self.done if "error" not in r.result and not r.result.get("cancelled")]
-        cancelled = sum(1 for r in self.done if r.result.get("cancelled"))
-        if not served:
-            return {"requests": 0, "failed": len(self.done) - cancelled, "cancelled": cancelled}
-        ttr = np.array([r.finished - r.arrival for r in served])
-        span = max(r.finished for r in served) - min(r.arrival for r in served)
-        cu = sum(int(r.cfg.rows) * int(r.cfg.cols) * int(r.result["steps"]) for r in served)
-        return {
-            "requests": len(served),
-            "failed": len(self.done) - len(served) - cancelled,
-            "cancelled": cancelled,
-            "p50_s": float(np.percentile(ttr, 50)),
-            "p99_s": float(np.percentile(ttr, 99)),
-            "mean_s": float(ttr.mean()),
-            "scenarios_per_hour": len(self.done) / span * 3600.0 if span > 0 else None,
-            "cell_updates_per_s": cu / span if span > 0 else None,
-            "peak_bytes": int(self.peak_bytes),
-            "ticks": self.ticks,
-            "span_s": float(span),
-        }
+        return summarize(self.done, self.peak_bytes, self.ticks)
+
+
+def summarize(done, peak_bytes, ticks):
+    """p50/p99/mean time to result, scenarios/hour, cell-updates/s and peak
+    bytes of a finished serving run (requests with their results)."""
+    if not done:
+        return {"requests": 0}
+    served = [r for r in done if "error" not in r.result and not r.result.get("cancelled")]
+    cancelled = sum(1 for r in done if r.result.get("cancelled"))
+    if not served:
+        return {"requests": 0, "failed": len(done) - cancelled, "cancelled": cancelled}
+    ttr = np.array([r.finished - r.arrival for r in served])
+    span = max(r.finished for r in served) - min(r.arrival for r in served)
+    cu = sum(int(r.cfg.rows) * int(r.cfg.cols) * int(r.result["steps"]) for r in served)
+    return {
+        "requests": len(served),
+        "failed": len(done) - len(served) - cancelled,
+        "cancelled": cancelled,
+        "p50_s": float(np.percentile(ttr, 50)),
+        "p99_s": float(np.percentile(ttr, 99)),
+        "mean_s": float(ttr.mean()),
+        "scenarios_per_hour": len(done) / span * 3600.0 if span > 0 else None,
+        "cell_updates_per_s": cu / span if span > 0 else None,
+        "peak_bytes": int(peak_bytes),
+        "ticks": ticks,
+        "span_s": float(span),
+    }
+
+
+class NativeServer:
+    """The same serving run through the library's own loop (sw2d_server_*,
+    C++ in libsw2d): admission, advancing and retirement happen there; this
+    class submits each request when its arrival time comes, records arrival
+    and completion times, keeps the results asked for and computes the
+    statistics.  `server_factory` returns a ServerHandle (or a stand-in with
+    its methods); its keep_depth must be set when keep_results asks for
+    depth rasters."""
+
+    def __init__(self, server_factory: Callable[[], object], keep_results=False,
+                 clock: Callable[[], float] = time.perf_counter, sleep: Callable[[float], None] = time.sleep):
+        from .native import REQ_CANCELLED, REQ_DONE, REQ_FAILED, REQ_PENDING
+        self._done_states = (REQ_DONE, REQ_FAILED, REQ_CANCELLED)
+        self._REQ_DONE, self._REQ_FAILED, self._REQ_PENDING = REQ_DONE, REQ_FAILED, REQ_PENDING
+        self.server = server_factory()
+        self.keep_results = keep_results
+        self.clock = clock
+        self.sleep = sleep
+        self.pending: list = []   # heap of (arrival, rid, Request) not yet arrived
+        self.active: dict = {}    # native request id -> Request
+        self.done: list = []
+        self.peak_bytes = 0
+        self.ticks = 0
+        self.t0 = None
+
+    def close(self):
+        close = getattr(self.server, "close", None)
+        if close:
+            close()
+
+    def submit(self, req: Request):
+        heapq.heappush(self.pending, (req.arrival, req.rid, req))
+
+    def now(self):
+        return self.clock() - self.t0
+
+    def _arrivals(self):
+        while self.pending and self.pending[0][0] <= self.now():
+            req = heapq.heappop(self.pending)[2]
+            try:
+                nid = self.server.submit(req.cfg, req.z, req.depth, manning=req.manning, rain_kind=req.rain_kind,
+                                         rain=req.rain, rain_dt=req.rain_dt, t_end=req.t_end)
+            except (SW2DError, ValueError) as e:  # refused (larger than the whole budget, bad arguments)
+                req.admitted = req.finished = self.now()
+                req.result = {"error": str(e)}
+                self.done.append(req)
+                continue
+            self.active[nid] = req
+
+    def step(self):
+        """Submit the arrived requests, run one round of the native loop, collect the finished ones."""
+        if self.t0 is None:
+            self.t0 = self.clock()
+        self._arrivals()
+        if not self.active:
+            return False
+        self.server.step()
+        self.ticks += 1
+        self.peak_bytes = max(self.peak_bytes, int(self.server.bytes_in_use()))
+        now = self.now()
+        for nid, req in list(self.active.items()):
+            st = self.server.poll(nid)
+            if req.admitted is None and st["state"] != self._REQ_PENDING:
+                req.admitted = now
+            if st["state"] not in self._done_states:
+                continue
+            if st["state"] == self._REQ_DONE:
+                res = {"t": st["t"], "steps": st["steps"], "budget": self.server.budget(nid)}
+                keep = self.keep_results(req) if callable(self.keep_results) else self.keep_results
+                if keep:
+                    res["depth"] = self.server.depth(nid)
+            elif st["state"] == self._REQ_FAILED:
+                res = {"error": self.server.request_error(nid)}
+            else:
+                res = {"cancelled": True}
+            req.result, req.finished = res, now
+            self.server.release(nid)
+            del self.active[nid]
+            self.done.append(req)
+        return True
+
+    def run(self, requests=(), timeout=None):
+        """Serves `requests` (plus anything submitted before) until all are done."""
+        for r in requests:
+            self.submit(r)
+        if self.t0 is None:
+            self.t0 = self.clock()
+        while self.pending or self.active:
+            if timeout is not None and self.now() > timeout:
+                raise TimeoutError(f"{len(self.pending)} waiting to arrive and {len(self.active)} in the server "
+                                   f"after {timeout} s")
+            if not self.step():
+                nxt = self.pending[0][0] - self.now()
+                if nxt > 0:
+                    self.sleep(min(nxt, 0.05))
+        return self.stats()
+
+    def stats(self):
+        return summarize(self.done, self.peak_bytes, self.ticks)
 
 
 def poisson_arrivals(rate, n, seed):

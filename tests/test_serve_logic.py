@@ -186,3 +186,90 @@ def test_poll_and_cancel():
     st = srv.stats()
     assert srv.poll(0) == "done"
     assert st["requests"] == 1 and st["cancelled"] == 2 and st["failed"] == 0
+
+
+class FakeServerHandle:
+    """Stands in for ServerHandle with the native loop's rules: submission
+    order, admission while `slots` and `budget` allow, `launches` per step,
+    a request's end after `t_end` launches; time advances by tick_cost."""
+
+    def __init__(self, clock, slots=2, budget=100, launches=10, tick_cost=0.1):
+        self.clock, self.slots, self.limit, self.launches, self.tick_cost = clock, slots, budget, launches, tick_cost
+        self.req, self.queue, self.next_id, self.used, self.released = {}, [], 1, 0, []
+
+    def submit(self, cfg, z, depth, manning=None, rain_kind=0, rain=None, rain_dt=1.0, t_end=1e300):
+        from sw2d import SW2DError
+        nbytes = getattr(cfg, "nbytes", 10)
+        if nbytes > self.limit:
+            raise SW2DError(1, "the request needs more device memory than the whole budget")
+        rid = self.next_id
+        self.next_id += 1
+        self.req[rid] = {"state": 1, "left": int(t_end), "steps": 0, "bytes": nbytes}
+        self.queue.append(rid)
+        return rid
+
+    def step(self):
+        running = [r for r, v in self.req.items() if v["state"] == 2]
+        for rid in list(self.queue):
+            v = self.req[rid]
+            if len(running) < self.slots and self.used + v["bytes"] <= self.limit:
+                v["state"] = 2
+                self.used += v["bytes"]
+                running.append(rid)
+                self.queue.remove(rid)
+        self.clock.t += self.tick_cost
+        for rid in running:
+            v = self.req[rid]
+            k = min(self.launches, v["left"])
+            v["left"] -= k
+            v["steps"] += k
+            if v["left"] == 0:
+                v["state"] = 3
+                self.used -= v["bytes"]
+        return len(self.queue), sum(1 for v in self.req.values() if v["state"] == 2)
+
+    def poll(self, rid):
+        v = self.req.get(rid)
+        return {"state": v["state"] if v else 0, "t": float(v["steps"]) if v else 0.0, "steps": v["steps"] if v else 0}
+
+    def budget(self, rid):
+        return {"steps": self.req[rid]["steps"]}
+
+    def depth(self, rid):
+        return np.full((1, 1), float(rid))
+
+    def request_error(self, rid):
+        return ""
+
+    def release(self, rid):
+        self.released.append(rid)
+        del self.req[rid]
+
+    def bytes_in_use(self):
+        return self.used
+
+
+def test_native_driver_submits_on_arrival_and_collects():
+    from sw2d import serve
+    clk = FakeClock()
+    fh = FakeServerHandle(clk, slots=2, budget=100, launches=10)
+    srv = serve.NativeServer(lambda: fh, keep_results=lambda r: r.rid % 2 == 0, clock=clk, sleep=clk.sleep)
+    arr = [0.0, 0.0, 0.0, 0.35, 2.0]
+    reqs = [_req(serve, k, a, 20 + 10 * k, 10) for k, a in enumerate(arr)]
+    big = _req(serve, 9, 0.5, 10, 10)
+    big.cfg = type("BigCfg", (), {"rows": 10, "cols": 10, "nbytes": 500})()
+    st = srv.run(reqs + [big])
+    assert st["requests"] == 5 and st["failed"] == 1
+    assert not srv.active and not srv.pending and sorted(fh.released) == [1, 2, 3, 4, 5]
+    for r in srv.done:
+        if r.rid == 9:
+            assert "error" in r.result
+            continue
+        assert r.finished >= r.admitted >= r.arrival
+        assert r.result["steps"] == r.t_end
+        assert ("depth" in r.result) == (r.rid % 2 == 0)
+    # two slots: the third request waits for the first to finish
+    third = next(r for r in srv.done if r.rid == 2)
+    first = next(r for r in srv.done if r.rid == 0)
+    assert third.admitted >= first.finished
+    assert srv.peak_bytes <= 100 and st["p50_s"] <= st["p99_s"]
