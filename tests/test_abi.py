@@ -113,6 +113,16 @@ int main(void) {
     cfg.rows = cfg.cols = 64;
     cfg.dx = cfg.dy = 1.0;
     if (sw2d_device_bytes(&cfg, &n) != SW2D_OK || n <= 0) return 4;
+    /* the serving loop's configuration, and a bad one refused before any device call */
+    sw2d_server_config sc;
+    if (sw2d_server_config_init(&sc) != SW2D_OK || sc.launches_per_step != 24 || sc.keep_depth != 1 ||
+        sc.batch.max_scenarios < 1)
+        return 5;
+    sc.launches_per_step = 0;
+    sw2d_server *srv = NULL;
+    if (sw2d_server_create(&sc, &srv) != SW2D_ERR_INVALID_ARG || srv != NULL) return 6;
+    int32_t state = -1;
+    if (sw2d_server_poll(NULL, 1, &state, NULL, NULL) != SW2D_ERR_INVALID_ARG) return 7;
     printf("%s|%s|%lld\n", sw2d_status_string(SW2D_OK), sw2d_status_string(SW2D_ERR_NONFINITE), (long long)n);
     return 0;
 }
