@@ -88,10 +88,21 @@ cudaError_t launch_batch(sw2d_batch *b, int slot) {
     B.scen = b->d_scen;
     B.units = b->d_units;
     B.hdr = b->d_hdr;
+    // a programmatic dependent of the launch before it: its CTAs are
+    // scheduled while that one drains, and wait for it to complete
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(b->grid);
+    lc.dynamicSmemBytes = 0;
+    lc.stream = b->stream;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
 #define SW2D_BL(id, nw, mb, un)                                                                 \
     if (b->cfg.variant == id) {                                                                 \
-        batch_step_kernel<nw, mb, un><<<b->grid, nw * 32, 0, b->stream>>>(B, slot);             \
-        return cudaGetLastError();                                                              \
+        lc.blockDim = dim3(nw * 32);                                                            \
+        return cudaLaunchKernelEx(&lc, batch_step_kernel<nw, mb, un>, B, slot);                 \
     }
     SW2D_BATCH_VARIANTS(SW2D_BL)
 #undef SW2D_BL

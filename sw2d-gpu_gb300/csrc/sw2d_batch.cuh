@@ -67,6 +67,12 @@ __device__ inline void write_status(const Clock &c, ScenarioStatus *st) {
 
 template <int NWARP, int MINB, int UNR>
 __global__ void __launch_bounds__(NWARP * 32, MINB) batch_step_kernel(const BatchDev B, const int slot) {
+    // Launched as a programmatic dependent of the previous iteration: wait
+    // until that grid has completed and its writes are visible (the queue
+    // head, every scenario's state and clock), then let the next iteration's
+    // grid be scheduled; its CTAs wait here the same way
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     __shared__ int s_sr[NWARP][kStreamMaxSrc], s_sc[NWARP][kStreamMaxSrc];
     __shared__ float s_q0[NWARP][kStreamMaxSrc], s_q1[NWARP][kStreamMaxSrc];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -74,6 +80,9 @@ __global__ void __launch_bounds__(NWARP * 32, MINB) batch_step_kernel(const Batc
     const int slot_nx = slot == 0 ? 2 : slot - 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) B.hdr->head[slot_out] = 0u;  // queue of the next launch
     const int n_units = B.hdr->n_units;
+    // with fewer units than warps, the warps past the unit count would only
+    // find the queue empty: the first n_units warps pull every unit
+    if ((int)blockIdx.x * NWARP + wid >= n_units) return;
     for (;;) {
         unsigned u = 0;
         if (lane == 0) u = atomicAdd(&B.hdr->head[slot], 1u);
