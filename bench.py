@@ -258,7 +258,9 @@ def run_ours(args):
     accuracy = fp32_vs_fp64(sw2d, s, spun, dev)
 
     # ---- end to end through the C ABI with host buffers ----------------------
-    k_e2e = max(3, args.steps)  # as many advances as timed steps, so the one-time upload is amortised
+    # as many advances as timed steps and at least 20, so that the one-time
+    # upload is amortised over a run of some length whatever --steps is
+    k_e2e = max(20, args.steps)
     h_pinned = torch.from_numpy(s["h0"]).pin_memory()
     z_pinned = torch.from_numpy(s["z"]).pin_memory()
     n_pinned = torch.from_numpy(s["n"]).pin_memory()
