@@ -186,3 +186,28 @@ def test_native_server_cancel_release_and_keep_depth(sw2d_mod):
         assert srv.budget(d)["steps"] > 0
         with pytest.raises(sw2d_mod.SW2DError):  # keep_depth = 0: no raster kept
             srv.depth(d)
+
+
+@pytest.mark.gpu
+def test_native_server_request_refused_at_admission_fails_alone(sw2d_mod):
+    """A request whose work units do not fit the batch's unit table is refused
+    by the batch at admission: it fails alone, with the batch's reason, its
+    device memory goes back, and the request behind it is served."""
+    from sw2d import native
+    small, big = _scn(90, 64, 64), _scn(91, 128, 128)
+    with sw2d_mod.ServerHandle(chunk=6, launches_per_step=6, max_units=30) as srv:  # 12 units fit, 40 do not
+        rb = srv.submit(_cfg(sw2d_mod, 128, 128), big["z"], big["h0"], manning=big["n"],
+                        rain_kind=sw2d_mod.RAIN_LINEAR, rain=RAIN, rain_dt=300.0, t_end=60.0)
+        rs = srv.submit(_cfg(sw2d_mod, 64, 64), small["z"], small["h0"], manning=small["n"],
+                        rain_kind=sw2d_mod.RAIN_LINEAR, rain=RAIN, rain_dt=300.0, t_end=60.0)
+        for _ in range(1000):
+            if srv.step() == (0, 0):
+                break
+        assert srv.poll(rb)["state"] == sw2d_mod.REQ_FAILED
+        assert "unit table" in srv.request_error(rb)
+        assert srv.poll(rs)["state"] == sw2d_mod.REQ_DONE
+        b = C.c_void_p()
+        assert native.load().sw2d_server_get_batch(srv._h, C.byref(b)) == native.OK
+        used = C.c_int64()
+        assert native.load().sw2d_batch_bytes_in_use(b, C.byref(used)) == native.OK
+        assert used.value == 0 and srv.bytes_in_use() == 0
