@@ -14,6 +14,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -132,7 +133,11 @@ int retire(sw2d_server *s) {
         rc = sw2d_batch_get_budget(s->batch, r.scenario, &r.budget);
         if (rc) return from_batch(s, rc, "budget");
         if (s->cfg.keep_depth) {
-            r.result.resize((size_t)r.cfg.rows * r.cfg.cols);
+            try {
+                r.result.resize((size_t)r.cfg.rows * r.cfg.cols);
+            } catch (...) {  // the request stays resident; a later step retries
+                return sfail(s, SW2D_ERR_OOM, "host memory for a finished request's depth");
+            }
             rc = sw2d_batch_get_field(s->batch, r.scenario, SW2D_FIELD_DEPTH, r.result.data());
             if (rc) return from_batch(s, rc, "depth");
         }
@@ -163,7 +168,8 @@ int sw2d_server_create(const sw2d_server_config *cfg, sw2d_server **out) {
     if (!cfg || !out) return SW2D_ERR_INVALID_ARG;
     *out = nullptr;
     if (cfg->launches_per_step < 1 || (cfg->keep_depth != 0 && cfg->keep_depth != 1)) return SW2D_ERR_INVALID_ARG;
-    sw2d_server *s = new sw2d_server();
+    sw2d_server *s = new (std::nothrow) sw2d_server();
+    if (!s) return SW2D_ERR_OOM;
     s->cfg = *cfg;
     const int rc = sw2d_batch_create(&cfg->batch, &s->batch);
     if (rc) {
@@ -196,33 +202,44 @@ int sw2d_server_submit(sw2d_server *s, const sw2d_config *cfg, const double *z, 
     if (s->cfg.batch.max_bytes > 0 && bytes > s->cfg.batch.max_bytes)
         return sfail(s, SW2D_ERR_INVALID_ARG, "the request needs more device memory than the whole budget");
     const size_t cells = (size_t)cfg->rows * cfg->cols;
-    const int32_t id = s->next_id++;
-    ServeRequest &r = s->req[id];
-    r.cfg = *cfg;
-    r.z.assign(z, z + cells);
-    if (manning) r.manning.assign(manning, manning + cells);
-    r.depth.assign(depth, depth + cells);
-    if (nr > 0) r.rain.assign(rain, rain + nr);
-    r.rain_kind = rain_kind;
-    r.n_rain = nr;
-    r.rain_dt = rain_dt;
-    r.t_end = t_end;
-    r.bytes = bytes;
-    std::memset(&r.budget, 0, sizeof(r.budget));
-    s->pending.push_back(id);
+    const int32_t id = s->next_id;
+    try {  // no exception crosses the C ABI: a failed host copy is SW2D_ERR_OOM
+        ServeRequest r;
+        r.cfg = *cfg;
+        r.z.assign(z, z + cells);
+        if (manning) r.manning.assign(manning, manning + cells);
+        r.depth.assign(depth, depth + cells);
+        if (nr > 0) r.rain.assign(rain, rain + nr);
+        r.rain_kind = rain_kind;
+        r.n_rain = nr;
+        r.rain_dt = rain_dt;
+        r.t_end = t_end;
+        r.bytes = bytes;
+        std::memset(&r.budget, 0, sizeof(r.budget));
+        s->req[id] = std::move(r);
+        s->pending.push_back(id);
+    } catch (...) {
+        s->req.erase(id);
+        return sfail(s, SW2D_ERR_OOM, "host memory for the request's copy");
+    }
+    s->next_id++;
     *request = id;
     return SW2D_OK;
 }
 
 int sw2d_server_step(sw2d_server *s, int32_t *pending, int32_t *running) {
     if (!s) return SW2D_ERR_INVALID_ARG;
-    int rc = admit(s);
-    if (rc) return rc;
-    if (!s->resident.empty()) {
-        rc = sw2d_batch_advance(s->batch, s->cfg.launches_per_step, nullptr);
-        if (rc) return from_batch(s, rc, "advance");
-        rc = retire(s);
+    try {  // no exception crosses the C ABI (host allocations of the bookkeeping)
+        int rc = admit(s);
         if (rc) return rc;
+        if (!s->resident.empty()) {
+            rc = sw2d_batch_advance(s->batch, s->cfg.launches_per_step, nullptr);
+            if (rc) return from_batch(s, rc, "advance");
+            rc = retire(s);
+            if (rc) return rc;
+        }
+    } catch (...) {
+        return SW2D_ERR_OOM;
     }
     if (pending) *pending = (int32_t)s->pending.size();
     if (running) *running = (int32_t)s->resident.size();
