@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -368,7 +369,8 @@ int sw2d_create(const sw2d_config *cfg, sw2d_handle **out) {
     *out = nullptr;
     std::string why;
     if (!validate(cfg, &why)) return SW2D_ERR_INVALID_ARG;
-    sw2d_handle *h = new sw2d_handle();
+    sw2d_handle *h = new (std::nothrow) sw2d_handle();  // no exception crosses the C ABI
+    if (!h) return SW2D_ERR_OOM;
     h->cfg = *cfg;
     h->real_size = cfg->precision == SW2D_PREC_F64 ? 8 : 4;
     grid_shape(cfg, &h->pitch, &h->plane, &h->tile_h, &h->tile_w);

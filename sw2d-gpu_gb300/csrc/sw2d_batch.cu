@@ -11,6 +11,7 @@
 // its own handle.
 #include <cmath>
 #include <cstring>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -139,10 +140,14 @@ int capture(sw2d_batch *b, int parity) {
 
 int upload_units(sw2d_batch *b) {
     b->units.clear();
-    for (size_t s = 0; s < b->scen.size(); s++) {
-        const HostScenario &h = b->scen[s];
-        if (!h.active) continue;
-        for (int u = 0; u < h.nunits; u++) b->units.push_back(make_int2((int)s, u));
+    try {  // no exception crosses the C ABI
+        for (size_t s = 0; s < b->scen.size(); s++) {
+            const HostScenario &h = b->scen[s];
+            if (!h.active) continue;
+            for (int u = 0; u < h.nunits; u++) b->units.push_back(make_int2((int)s, u));
+        }
+    } catch (...) {
+        return bfail(b, SW2D_ERR_OOM, "host memory for the unit table");
     }
     if ((long long)b->units.size() > b->cfg.max_units)
         return bfail(b, SW2D_ERR_INVALID_ARG, "unit table full: raise max_units");
@@ -210,7 +215,8 @@ int sw2d_batch_create(const sw2d_batch_config *cfg, sw2d_batch **out) {
     if (cfg->max_scenarios < 1 || cfg->max_units < 1 || cfg->chunk < 3 || cfg->chunk % 3 != 0 || cfg->strip_h < 0 ||
         cfg->variant < 0 || cfg->variant >= kBatchVariants)
         return SW2D_ERR_INVALID_ARG;
-    sw2d_batch *b = new sw2d_batch();
+    sw2d_batch *b = new (std::nothrow) sw2d_batch();  // no exception crosses the C ABI
+    if (!b) return SW2D_ERR_OOM;
     b->cfg = *cfg;
     auto bail = [&](int code) {
         sw2d_batch_destroy(b);
@@ -231,7 +237,11 @@ int sw2d_batch_create(const sw2d_batch_config *cfg, sw2d_batch **out) {
     cudaMemset(b->d_hdr, 0, sizeof(BatchHeader));
     cudaMemset(b->d_scen, 0, (size_t)cfg->max_scenarios * sizeof(ScenarioDev));
     cudaMemset(b->d_status, 0, (size_t)cfg->max_scenarios * sizeof(ScenarioStatus));
-    b->scen.resize(cfg->max_scenarios);
+    try {
+        b->scen.resize(cfg->max_scenarios);
+    } catch (...) {
+        return bail(SW2D_ERR_OOM);
+    }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg->device);
     int per_sm = batch_ctas_per_sm(cfg->variant);
