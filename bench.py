@@ -187,7 +187,7 @@ def run_ours(args):
     tuned_b = autotune.tune_batch(device=dev) if (args.batched or args.served) else {}
     tune_s = time.perf_counter() - t_tune
     log(f"[rank {rank}] autotune: strip_h={tuned['strip_h']} variant={tuned['variant']} "
-        f"batch={tuned_b.get('variant')}/{tuned_b.get('chunk')} ({tune_s:.1f}s, "
+        f"batch={tuned_b.get('variant')}/{tuned_b.get('chunk')}/{tuned_b.get('strip_h')} ({tune_s:.1f}s, "
         f"{len(tuned.get('timings', []))} + {len(tuned_b.get('timings', []))} candidates)")
 
     g = make_solver(sw2d, s, sw2d.PREC_F32, dev)
@@ -317,6 +317,7 @@ def run_ours(args):
                        "seed": SEED,
                        "autotuned": {"strip_h": tuned["strip_h"], "variant": tuned["variant"], "kernel": kernel_desc,
                                      "batch_variant": tuned_b.get("variant"), "batch_chunk": tuned_b.get("chunk"),
+                                     "batch_strip_h": tuned_b.get("strip_h"),
                                      "steps_per_launch": steps_per_launch(kernel_desc), "tuning_s": tune_s,
                                      "candidates": len(tuned.get("timings", [])) + len(tuned_b.get("timings", []))}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -405,7 +406,7 @@ def run_batched(sw2d, dev, args, rank=0, ws=1):
     ens_all = S.ensemble(terrain_bank(), count=args.batch_count, seed=SEED + 11)
     ens = [ens_all[k] for k in replicas.shard(len(ens_all), rank, ws)]
     t0 = time.perf_counter()
-    b = sw2d.Batch(device=dev, max_scenarios=len(ens) + 8)  # build and chunk: the autotuner's
+    b = sw2d.Batch(device=dev, max_scenarios=len(ens) + 8)  # build, chunk and strip height: the autotuner's
     ids = [b.add(scen_cfg(sw2d, e["side"], device=dev), e["z"], e["h0"], manning=e["n"],
                  rain_kind=sw2d.RAIN_LINEAR, rain=e["rain"], rain_dt=e["rain_dt"], t_end=e["t_end"]) for e in ens]
     t_admit = time.perf_counter() - t0

@@ -50,6 +50,11 @@ def wave_strips(rows: int, cols: int, sms: int = 152, waves=(1, 2, 3, 4), warps_
 
 
 BATCH_VARIANTS = (0, 1, 2)
+# rows per warp for every scenario of a batch (0: by scenario size, 16/32/64
+# rows); taller strips repeat fewer warm-up rows, which pays on a large
+# ensemble (measured on GB300, 64 scenarios of 128-1024 cells a side: 4.85e10
+# cell-updates/s by size, 4.98e10 with 64 rows, 5.02e10 with 96)
+BATCH_STRIPS = (0, 64, 96)
 BATCH_CLASS = "batch"
 STEPS_PER_LAUNCH = (1, 24, 48, 96)  # fixed time step: iterations per launch tried by tune_fixed
 FIXED_VARIANTS = (0, 2)
@@ -236,7 +241,7 @@ def _batch_timer(device, count, launches):
 
     def timer(c):
         b = sw2d.Batch(sw2d.batch_config(device=device, chunk=c["chunk"], variant=c["variant"],
-                                         max_scenarios=count + 1))
+                                         strip_h=c.get("strip_h", 0), max_scenarios=count + 1))
         try:
             for e in ens:
                 cfg = sw2d.default_config(rows=e["side"], cols=e["side"], dx=5.0, dy=5.0, precision=sw2d.PREC_F32,
@@ -255,26 +260,43 @@ def _batch_timer(device, count, launches):
 
 
 def tune_batch(device: int = 0, cache: Optional[Cache] = None, variants=BATCH_VARIANTS, chunks=(12, 24, 48),
-               count: int = 24, launches: int = 96, force: bool = False) -> dict:
-    """Best (batched-kernel build, graph chunk) on a small wet ensemble (cached)."""
+               strips=BATCH_STRIPS, count: int = 24, launches: int = 96, force: bool = False) -> dict:
+    """Best (batched-kernel build, graph chunk), then the best strip height
+    for that pair, on a small wet ensemble (cached)."""
     cache = cache or Cache()
     gpu = f"{gpu_name(device)}|{TABLE_VERSION}"
     hit = cache.get(gpu, BATCH_CLASS)
     if hit and not force:
         return hit
-    cands = [{"variant": v, "chunk": ch} for v in variants for ch in chunks]
-    best, table = search(cands, _batch_timer(device, count, launches))
+    timer = _batch_timer(device, count, launches)
+    cands = [{"variant": v, "chunk": ch, "strip_h": 0} for v in variants for ch in chunks]
+    best, table = search(cands, timer)
+    others = [sh for sh in strips if sh != 0]
+    if others:
+        pair = {"variant": best["variant"], "chunk": best["chunk"]}
+        t_best = min(r["s_per_iter"] for r in table if "s_per_iter" in r)
+        try:
+            best2, table2 = search([{**pair, "strip_h": sh} for sh in others], timer)
+        except RuntimeError:  # none of the taller strips ran: keep the size rule
+            best2, table2 = None, []
+        table = table + table2
+        ok2 = [r["s_per_iter"] for r in table2 if "s_per_iter" in r]
+        if best2 is not None and ok2 and min(ok2) < t_best:
+            best = best2
     entry = {**best, "timings": table}
     cache.put(gpu, BATCH_CLASS, entry)
     return entry
 
 
 def apply_batch(bcfg, cache: Optional[Cache] = None):
-    """Fills bcfg.variant / bcfg.chunk from the cache; returns bcfg."""
+    """Fills bcfg.variant / bcfg.chunk (and strip_h, when the cached choice
+    has one and bcfg leaves it to the library) from the cache; returns bcfg."""
     hit = (cache or Cache()).get(f"{gpu_name(bcfg.device)}|{TABLE_VERSION}", BATCH_CLASS)
     if hit:
         bcfg.variant = int(hit["variant"])
         bcfg.chunk = int(hit["chunk"])
+        if bcfg.strip_h == 0:
+            bcfg.strip_h = int(hit.get("strip_h", 0))
     return bcfg
 
 

@@ -31,6 +31,7 @@ def main():
     ap.add_argument("--iters", type=int, default=96)
     ap.add_argument("--variant", type=int, default=-1, help="-1: the library's (or the autotuner's) choice")
     ap.add_argument("--chunk", type=int, default=0, help="graph length; 0: the library's choice")
+    ap.add_argument("--strip-h", type=int, default=0, help="rows per warp for every scenario; 0: by scenario size")
     ap.add_argument("--seed", type=int, default=1)
     a = ap.parse_args()
     bank = S.TerrainBank(size=max(2048, max(a.sides)), dx=5.0, seed=a.seed)
@@ -40,6 +41,8 @@ def main():
         kw["variant"] = a.variant
     if a.chunk > 0:
         kw["chunk"] = a.chunk
+    if a.strip_h > 0:
+        kw["strip_h"] = a.strip_h
     with sw2d.Batch(device=0, max_scenarios=a.count, **kw) as b:
         ids = []
         for e in ens:

@@ -91,10 +91,11 @@ def test_batch_tuning_picks_a_build_and_chunk(sw2d_mod, tmp_path, monkeypatch):
     from sw2d import autotune
     from sw2d import scenarios as S
     monkeypatch.setenv("SW2D_AUTOTUNE_CACHE", str(tmp_path / "t.json"))
-    best = autotune.tune_batch(variants=(0, 2), chunks=(6, 12), count=4, launches=24)
-    assert best["variant"] in (0, 2) and best["chunk"] in (6, 12) and len(best["timings"]) == 4
+    best = autotune.tune_batch(variants=(0, 2), chunks=(6, 12), strips=(0, 64), count=4, launches=24)
+    assert best["variant"] in (0, 2) and best["chunk"] in (6, 12) and best["strip_h"] in (0, 64)
+    assert len(best["timings"]) == 5
     b = sw2d_mod.Batch(max_scenarios=4)
-    assert (b.cfg.variant, b.cfg.chunk) == (best["variant"], best["chunk"])
+    assert (b.cfg.variant, b.cfg.chunk, b.cfg.strip_h) == (best["variant"], best["chunk"], best["strip_h"])
     b.close()
     s = S.catchment(96, dx=5.0, seed=2)
     depth = {}
@@ -150,3 +151,38 @@ def test_tune_fixed_on_gpu(sw2d_mod, tmp_path):
     g = sw2d_mod.Solver(cfg)
     assert f"steps_per_launch={best['steps_per_launch']}" in g.describe()
     g.close()
+
+
+def test_batch_tuning_then_strip_height_on_the_host(tmp_path, monkeypatch):
+    """tune_batch picks the (build, chunk) pair with the size rule for the
+    strips, then tries the taller strips for that pair only and keeps them
+    when faster; apply_batch fills strip_h only where the caller left it to
+    the library (fake timer, no GPU)."""
+    from sw2d import autotune
+    times = {(0, 12, 0): 3.0, (0, 24, 0): 2.0, (1, 12, 0): 2.5, (1, 24, 0): 2.2, (0, 24, 64): 1.9, (0, 24, 96): 1.7}
+    seen = []
+
+    def fake_timer(device, count, launches):
+        def t(c):
+            seen.append((c["variant"], c["chunk"], c["strip_h"]))
+            return times[seen[-1]]
+        return t
+
+    monkeypatch.setattr(autotune, "_batch_timer", fake_timer)
+    monkeypatch.setattr(autotune, "gpu_name", lambda device=0: "fake-gpu")
+    monkeypatch.setenv("SW2D_AUTOTUNE_CACHE", str(tmp_path / "t.json"))
+    best = autotune.tune_batch(variants=(0, 1), chunks=(12, 24), strips=(0, 64, 96))
+    assert (best["variant"], best["chunk"], best["strip_h"]) == (0, 24, 96)
+    assert seen[-2:] == [(0, 24, 64), (0, 24, 96)] and len(seen) == 6  # strips only for the best pair
+
+    class B:  # the fields apply_batch reads and writes
+        device, variant, chunk, strip_h = 0, 0, 0, 0
+
+    b = autotune.apply_batch(B())
+    assert (b.variant, b.chunk, b.strip_h) == (0, 24, 96)
+    b = B()
+    b.strip_h = 32
+    assert autotune.apply_batch(b).strip_h == 32  # the caller's own strip height stays
+    times[(0, 24, 64)] = times[(0, 24, 96)] = 9.0  # taller strips slower: the size rule stays
+    best = autotune.tune_batch(variants=(0, 1), chunks=(12, 24), strips=(0, 64, 96), force=True)
+    assert best["strip_h"] == 0
